@@ -1,0 +1,350 @@
+"""Benchmark: random-layer state-vector sweep at N=28 (complex128) on GB300.
+
+Workload (one step): a seeded random circuit on N qubits, L layers, each
+layer = a Haar-random U(2) on every qubit then CZ on a random perfect
+matching (N=28, L=100: 4200 gates), run by ``Circuit.run`` from |0...0>.
+The state (16 * 2^28 B = 4 GiB) is far larger than L2, so every pass streams
+from HBM; no flush is needed between steps.
+
+Reported (one JSON line on rank 0):
+  value      effective gate GB/s = gates x (2 * 16 * 2^N bytes) / step time,
+             i.e. the HBM bandwidth an unfused simulator would need to match
+             this speed (fusion can lift it above the HBM peak);
+  roofline   the dominant kernel (fused tile pass): bytes actually moved per
+             launch (2 * 16 * 2^N) / its mean CUDA-event duration, against the
+             measured HBM copy bandwidth;
+  e2e        the same metric through the public API with the initial state
+             copied from pinned host memory and the final state read back;
+  cpu_baseline  the CPU oracle (numpy einsum, the reference numpy backend's
+             algorithm) on a bounded sample of the same circuit family.
+
+``--impl reference`` times the CPU oracle port alone on this workload.
+With ``torchrun --nproc-per-node N`` each rank runs an independent replica.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "gate GB/s vs HBM peak at N=28; QAOA time-to-0.9-ratio, learned vs plain init"
+
+
+def c2_circuit_ops(N, layers, seed):
+    """(kind, qubits, matrix) list: Haar U(2) on every qubit then CZ on a
+    seeded random perfect matching, per layer."""
+    import scipy.stats
+    rng = np.random.default_rng(seed)
+    ops = []
+    for _ in range(layers):
+        for q in range(N):
+            ops.append((1, (q,), scipy.stats.unitary_group.rvs(2, random_state=rng)))
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            ops.append((2, (int(perm[a]), int(perm[a + 1])), None))
+    return ops
+
+
+def build_circuit(ops):
+    import quantumflow_gb300 as qf
+    circ = qf.Circuit()
+    for kind, qs, u in ops:
+        circ += qf.Gate(u, qubits=qs) if kind == 1 else qf.CZ(*qs)
+    return circ
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"qf_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(ops, N, budget_s=12.0):
+    """CPU oracle (numpy einsum restatement of the reference numpy backend)
+    on a prefix of the same circuit family at N qubits; returns
+    (gate GB/s, gates timed, seconds)."""
+    from oracle import qf_oracle as orc
+    st = orc.zero_state(N)
+    cz = orc.CZ()
+    t0 = time.perf_counter()
+    done = 0
+    for kind, qs, u in ops:
+        st = orc.tensormul(u if kind == 1 else cz, st, list(qs))
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done * 2 * 16 * 2 ** N / dt / 1e9, done, dt
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU oracle port (the reference is pure Python; its
+    numpy backend's tensormul is np.einsum, restated in oracle/qf_oracle.py)."""
+    if rank != 0:
+        return
+    N = args.ref_n
+    ops = c2_circuit_ops(N, 1, args.seed)
+    from oracle import qf_oracle as orc
+    per_step = args.ref_gates
+    st = orc.zero_state(N)
+    cz = orc.CZ()
+
+    def step(st, k0):
+        for kind, qs, u in ops[k0:k0 + per_step]:
+            st = orc.tensormul(u if kind == 1 else cz, st, list(qs))
+        return st
+
+    for w in range(args.warmup):
+        st = step(st, 0)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        st = step(st, 0)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = per_step * 2 * 16 * 2 ** N / dt / 1e9
+    sample = (f"numpy einsum oracle port, N={N} complex128, {per_step} gates of layer 0 of the "
+              f"random-layer circuit per step, single thread (np.einsum)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 numpy)", "data": "synthetic",
+        "config": {"workload": f"random-layer circuit N={N} (Haar U(2) per qubit + CZ matching), "
+                               f"bounded sample of {per_step} gates per step"},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=28)
+    ap.add_argument("--layers", type=int, default=100)
+    ap.add_argument("--dtype", default="complex128", choices=["complex128", "complex64"])
+    ap.add_argument("--arith", default=None, choices=["ff", "fp64"])
+    ap.add_argument("--fusion", type=int, default=6)
+    ap.add_argument("--seed", type=int, default=2018)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-n", type=int, default=28)
+    ap.add_argument("--ref-gates", type=int, default=3)
+    ap.add_argument("--cpu-n", type=int, default=24)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    if args.arith:
+        os.environ["QUANTUMFLOW_GB300_C128"] = args.arith
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    if args.arith:
+        qf.config.C128_ARITHMETIC = args.arith
+
+    N, S = args.n, (16 if args.dtype == "complex128" else 8)
+    sweep_bytes = 2 * S * 2 ** N
+    ops = c2_circuit_ops(N, args.layers, args.seed)
+    circ = build_circuit(ops)
+    ngates = len(ops)
+
+    def step():
+        return circ.run(qf.zero_state(N, dtype=args.dtype), fusion_k=args.fusion)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ket = step()
+        del ket
+    torch.cuda.synchronize()
+    passes = circ.last_passes
+
+    # ---- timed region (device events on the launch stream) ------------
+    clocks = ClockSampler(local)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nat.timing_collect()
+    nat.timing_enable(True)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ket = step()
+        del ket
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clock_info = clocks.stop()
+    nat.timing_enable(False)
+    kt = nat.timing_collect()
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ngates * sweep_bytes / (ms * 1e-3) / 1e9
+    launches = sum(c for _, c in kt.values()) + args.steps  # + one |0> fill per step
+
+    peak, peak_kind = measured_peaks()
+    tile_ms, tile_n = kt["fused_tile"]
+    dom = "fused_tile" if tile_n else max(kt, key=lambda k: kt[k][0])
+    dom_ms, dom_n = kt[dom]
+    achieved = sweep_bytes / (dom_ms / dom_n * 1e-3) / 1e9 if dom_n else None
+    total_kernel_ms = sum(m for m, _ in kt.values())
+    roofline = {
+        "bound": "hbm", "kernel": f"k_tile ({dom})", "achieved": achieved, "peak": peak,
+        "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+        "traffic": None, "launches_timed": dom_n,
+        "share_of_kernel_time": dom_ms / total_kernel_ms if total_kernel_ms else None,
+        "bytes_per_launch": sweep_bytes,
+    }
+
+    # ---- end to end: host state in, host state out ----------------------
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        cdt = torch.complex128 if args.dtype == "complex128" else torch.complex64
+        host_in = torch.zeros(2 ** N, dtype=cdt).pin_memory()
+        host_in[0] = 1
+        host_out = torch.empty(2 ** N, dtype=cdt).pin_memory()
+
+        def e2e_step():
+            ket = qf.State(host_in.to("cuda", non_blocking=True), dtype=args.dtype)
+            ket = circ.run(ket, fusion_k=args.fusion)
+            host_out.copy_(ket.tensor.reshape(-1), non_blocking=True)
+            return ket
+
+        e2e_step()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(max(1, args.steps)):
+            k = e2e_step()
+            del k
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ems = f0.elapsed_time(f1) / max(1, args.steps)
+        nbytes = host_in.numel() * host_in.element_size()
+        e2e = {"value": ngates * sweep_bytes / (ems * 1e-3) / 1e9, "unit": "GB/s",
+               "ms_per_step": ems, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+        del host_in, host_out
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu_ops = c2_circuit_ops(args.cpu_n, 1, args.seed)
+        v, done, dt = cpu_oracle_rate(cpu_ops, args.cpu_n)
+        cpu = {"value": v, "unit": "GB/s", "cores": 1, "kind": "port",
+               "sample": f"numpy einsum oracle, N={args.cpu_n} complex128, first {done} gates of the "
+                         f"random-layer circuit ({dt:.1f} s, single thread)"}
+
+    if rank == 0:
+        arith = qf.config.C128_ARITHMETIC if args.dtype == "complex128" else "fp32"
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": {"ff": "c128 (float-float arithmetic)", "fp64": "c128 (FP64)",
+                      "fp32": "c64 (FP32)"}[arith],
+            "data": "synthetic",
+            "config": {"workload": f"random-layer circuit N={N}, {args.layers} layers x (Haar U(2) on "
+                                   f"every qubit + CZ on a seeded perfect matching), {ngates} gates, "
+                                   f"fusion k={args.fusion}",
+                       "state_bytes": S * 2 ** N, "l2": "state larger than L2 (no flush needed)",
+                       "parallelism": f"replicas x{world}"},
+            "gate_apps_per_s": world * ngates / (ms * 1e-3),
+            "passes_per_step": passes,
+            "pass_gbs": world * passes * sweep_bytes / (ms * 1e-3) / 1e9,
+            "roofline": roofline,
+            "kernel_ms_per_step": {k: m / args.steps for k, (m, c) in kt.items() if c},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clock_info,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/*
+ * qf_gb300.h -- C ABI of the GB300 state-vector backend for QuantumFlow.
+ *
+ * Plain pointers and sizes only: device pointers are CUDA global-memory
+ * addresses (any allocator), `stream` is a cudaStream_t (NULL = legacy default
+ * stream).  Every entry point returns a status code (QF_OK = 0); none aborts,
+ * traps or prints.  Calls are asynchronous on `stream` unless stated.
+ *
+ * Conventions shared with the reference (rigetti/quantumflow):
+ *   - A state on n qubits is 2^n complex amplitudes in C order, i.e. the
+ *     reference tensor of shape [2]*n flattened (quantumflow/qubits.py:63-84).
+ *     Reference axis a lives at bit (n-1-a) of the flat index: axis 0 is the
+ *     most significant bit.
+ *   - Qubit arguments are AXIS indices in that convention (the `indices`
+ *     argument of quantumflow/backend/numpybk.py:159 tensormul).
+ *   - A k-qubit gate matrix is the reference gate tensor [2]*(2k) reshaped to
+ *     (2^k, 2^k), row-major, gate qubit 0 the most significant bit of the row
+ *     and column index (quantumflow/qubits.py:70-80), passed as interleaved
+ *     (re, im) doubles: 2 * 4^k doubles.
+ *
+ * Element layouts (bytes per amplitude):
+ *   QF_LAYOUT_C64   complex64  (float re, float im)                 8
+ *   QF_LAYOUT_C128  complex128 (double re, double im), FP64 math   16
+ *   QF_LAYOUT_FF    complex128 value held as float-float pairs
+ *                   (re_hi, re_lo, im_hi, im_lo), 48-bit significand,
+ *                   float-float math on the FP32 pipes            16
+ */
+#ifndef QF_GB300_H
+#define QF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QF_ABI_VERSION 1
+
+#define QF_LAYOUT_C64 0
+#define QF_LAYOUT_C128 1
+#define QF_LAYOUT_FF 2
+
+#define QF_OK 0
+#define QF_ERR_INVALID_ARGUMENT 1 /* bad qubit index, k, n, null pointer, ... */
+#define QF_ERR_LAYOUT 2           /* unknown element layout                    */
+#define QF_ERR_CUDA 3             /* a CUDA runtime call failed                 */
+#define QF_ERR_ALIGNMENT 4        /* device pointer not 16-byte aligned         */
+#define QF_ERR_TOO_LARGE 5        /* n above QF_MAX_QUBITS or table too large   */
+#define QF_ERR_NOT_SUPPORTED 6    /* e.g. dense gate on more than 5 qubits      */
+#define QF_ERR_DEVICE 7           /* a bounded device-side wait gave up         */
+#define QF_ERR_WORKSPACE 8        /* workspace missing or too small             */
+
+#define QF_MAX_QUBITS 34
+#define QF_MAX_GATE_QUBITS 5
+
+/* ------------------------------------------------------------ utilities -- */
+int qf_abi_version(void);
+const char* qf_status_string(int status);
+/* cudaError_t of the most recent failing CUDA call made by this thread. */
+int qf_last_cuda_error(void);
+/* Read and clear the device error word (bit 0: a bounded wait gave up).
+ * Synchronises `stream`. */
+int qf_get_device_error(int* flags, void* stream);
+/* Bytes of workspace the reductions below need for an n-qubit state. */
+size_t qf_reduce_workspace_bytes(int n);
+
+/* ------------------------------------------------- kernel timing ---------- */
+/* Instrumentation with no counterpart in the reference (whose only timing is
+ * timeit in tools/benchmark.py:48-53).  While enabled, every engine kernel
+ * launched by qf_apply_gate / qf_run_circuit / qf_qaoa_state is bracketed by
+ * a CUDA event pair on its launch stream.  qf_timing_collect synchronises on
+ * the recorded events and returns, per kernel class, the summed milliseconds
+ * and the launch count since the previous collect. */
+#define QF_KERNEL_FUSED_TILE 0
+#define QF_KERNEL_DENSE1 1
+#define QF_KERNEL_DENSE2 2
+#define QF_KERNEL_PERMUTATION 3
+#define QF_KERNEL_ELEMENTWISE 4
+#define QF_KERNEL_CLASSES 5
+int qf_timing_enable(int on);
+int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
+
+/* ------------------------------------------------- state preparation ------ */
+/* psi = |index> (quantumflow/states.py:186-191 zero_state for index 0). */
+int qf_fill_basis(void* psi, int n, int layout, int64_t index, void* stream);
+/* psi = |+>^n = H^n |0..0>, the state after the H layer of
+ * quantumflow/qaoa.py:43-44. */
+int qf_fill_uniform(void* psi, int n, int layout, void* stream);
+/* Element-wise layout conversion (src and dst must not alias). */
+int qf_convert(const void* src, int src_layout, void* dst, int dst_layout, int n, void* stream);
+/* psi *= scale (real).  Used by State.normalize (quantumflow/states.py:108-111). */
+int qf_scale(void* psi, int n, int layout, double scale, void* stream);
+
+/* ------------------------------------------------- gate application ------- */
+/* psi_out = gate (.) psi_in on the given axes.  Replaces
+ * quantumflow/backend/numpybk.py:159-214 tensormul (called from
+ * quantumflow/ops.py:161-166 Gate.run).  psi_out may equal psi_in (in place).
+ * k = 1..QF_MAX_GATE_QUBITS, matrix = 2*4^k interleaved doubles (host). */
+int qf_apply_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
+                  const double* matrix, void* stream);
+
+/* Apply nops gates in order with gate fusion.  Replaces the per-gate loop of
+ * quantumflow/circuits.py:87-99 Circuit.run.  Gate i acts on op_k[i] axes
+ * taken consecutively from op_axes; its matrix is the next 2*4^k doubles of
+ * op_mats (host arrays).  fusion_k = maximum number of non-contiguous high
+ * qubits per fused pass (0 = library default, 1 = no fusion).  *passes (may
+ * be NULL) receives the number of full-state passes launched. */
+int qf_run_circuit(const void* psi_in, void* psi_out, int n, int layout, int nops, const int* op_k,
+                   const int* op_axes, const double* op_mats, int fusion_k, int* passes,
+                   void* stream);
+
+/* ------------------------------------------------------------- QAOA ------- */
+/* cuts[x] = number of edges cut by basis state x (unweighted graph),
+ * the table quantumflow/qaoa.py:68-81 graph_cuts builds in Python.
+ * edges = 2*nedges axis indices (device-independent host array). */
+int qf_cut_values(uint16_t* cuts, int n, int nedges, const int* edges, void* stream);
+/* Weighted variant: cuts[x] = sum of weights of cut edges (double). */
+int qf_cut_values_weighted(double* cuts, int n, int nedges, const int* edges, const double* weights,
+                           void* stream);
+
+/* The QAOA state of quantumflow/qaoa.py:22-64 qubo_circuit for an
+ * unweighted graph given its cut table: |+>^n, then for each of p steps the
+ * cost layer prod_e ZZ(-gamma/pi) = exp(i*gamma*(E/2 - C(x))) as one
+ * diagonal-phase pass, RZ(node_theta[q]) on nodes whose theta is not NaN
+ * (node_theta may be NULL), then RX(beta) on every node.  nedges = E. */
+int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p,
+                  const double* beta, const double* gamma, const double* node_theta, int fusion_k,
+                  void* stream);
+
+/* ------------------------------------------------------- reductions ------- */
+/* All reductions write their result to DEVICE memory `out` and need a
+ * workspace of qf_reduce_workspace_bytes(n) bytes (device, 256-byte aligned).
+ * Results are deterministic (fixed-order two-pass reduction). */
+
+/* out[0] = sum_x cuts[x] |psi_x|^2 -- State.expectation
+ * (quantumflow/states.py:131-147) with the diagonal of graph_cuts. */
+int qf_expectation_cuts(const void* psi, int n, int layout, const uint16_t* cuts, double* out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+/* out[0] = sum_x diag[x] |psi_x|^2 for a real device array diag[2^n]. */
+int qf_expectation_diag(const void* psi, int n, int layout, const double* diag, double* out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+/* out[0] = sum_x |psi_x|^2 (quantumflow/qubits.py:180-182 norm). */
+int qf_norm2(const void* psi, int n, int layout, double* out, void* workspace,
+             size_t workspace_bytes, void* stream);
+/* out[0..1] = (re, im) of <a|b> = sum_x conj(a_x) b_x
+ * (quantumflow/backend/numpybk.py:125-128 inner). */
+int qf_inner(const void* a, const void* b, int n, int layout, double* out, void* workspace,
+             size_t workspace_bytes, void* stream);
+/* probs[x] = |psi_x|^2 as double (quantumflow/states.py:113-119). */
+int qf_probabilities(const void* psi, int n, int layout, double* probs, void* stream);
+/* Multinomial sampling, quantumflow/states.py:121-129 State.sample:
+ * counts[x] (int64, device, 2^n, zeroed by the call) = number of the
+ * `trials` draws that gave x.  Draws use a counter-based generator keyed by
+ * `seed`.  Needs qf_sample_workspace_bytes(n) of workspace. */
+size_t qf_sample_workspace_bytes(int n);
+int qf_sample(const void* psi, int n, int layout, int64_t trials, uint64_t seed, int64_t* counts,
+              void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QF_GB300_H */

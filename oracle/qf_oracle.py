@@ -1,0 +1,199 @@
+"""CPU oracle for the quantumflow_gb300 parity tests -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg may import this module, and only as the checker (or the timed CPU
+baseline), never as a product path.  It is a numpy restatement of the
+reference QuantumFlow (rigetti/quantumflow) algorithms on the state-vector
+path; each function cites the reference file:line it restates.
+
+Parity pin: ``tests/golden/*.npz`` were produced by running the reference
+package itself (numpy backend) with ``tests/golden/make_golden.py``;
+``tests/test_oracle.py`` checks every function here against those outputs
+and against the literal known-answer vectors of the reference's own tests.
+"""
+import numpy as np
+
+EINSUM_SUBSCRIPTS = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
+
+
+# ------------------------------------------------------------ core ---------
+def tensormul(gate, state, indices):
+    """Contract a K-qubit gate with an N-axis tensor on ``indices``.
+
+    Restates quantumflow/backend/numpybk.py:159-214: the gate's bra axes are
+    summed against the state axes ``indices`` and its ket axes written back
+    at the same positions (out of place).  ``gate`` is (2^K, 2^K) or
+    [2]*2K; ``state`` is [2]*N or flat."""
+    gate = np.asarray(gate, dtype=np.complex128)
+    state = np.asarray(state, dtype=np.complex128)
+    K = len(indices)
+    N = int(round(np.log2(state.size)))
+    g = gate.reshape([2] * (2 * K))
+    s = state.reshape([2] * N)
+    out = list(EINSUM_SUBSCRIPTS[:N])
+    left_in = list(EINSUM_SUBSCRIPTS[N:N + K])
+    left_out = [out[i] for i in indices]
+    right = list(out)
+    for i, c in zip(indices, left_in):
+        right[i] = c
+    sub = "".join(left_out + left_in) + "," + "".join(right) + "->" + "".join(out)
+    return np.einsum(sub, g, s)
+
+
+def run_ops(state, ops):
+    """Apply (matrix, axes) pairs in order (quantumflow/circuits.py:87-99)."""
+    for m, axes in ops:
+        state = tensormul(m, state, list(axes))
+    return state
+
+
+def zero_state(n):
+    """|0...0> (quantumflow/states.py:186-191)."""
+    s = np.zeros(2 ** n, dtype=np.complex128)
+    s[0] = 1
+    return s.reshape([2] * n)
+
+
+def probabilities(state):
+    """|psi|^2 (quantumflow/states.py:113-119)."""
+    a = np.abs(state)
+    return a * a
+
+
+def expectation(state, diag):
+    """sum Re(h) p (quantumflow/states.py:131-147)."""
+    return float(np.sum(np.real(np.asarray(diag)).reshape(-1) * probabilities(state).reshape(-1)))
+
+
+def norm(state):
+    """|<psi|psi>| (quantumflow/qubits.py:180-182)."""
+    return float(np.abs(np.vdot(state, state)))
+
+
+def inner(a, b):
+    """np.vdot (quantumflow/backend/numpybk.py:125-128)."""
+    return complex(np.vdot(a, b))
+
+
+def fidelity(a, b):
+    """|<a|b>|^2 (quantumflow/measures.py:32-36)."""
+    return abs(inner(a, b)) ** 2
+
+
+# ------------------------------------------------------------ gates --------
+def cis(x):
+    return np.exp(1j * x)
+
+
+def H():
+    """quantumflow/stdgates.py:91-109."""
+    return np.array([[1, 1], [1, -1]], dtype=np.complex128) / np.sqrt(2)
+
+
+def X():
+    return np.array([[0, 1], [1, 0]], dtype=np.complex128)
+
+
+def T():
+    """quantumflow/stdgates.py:133-151."""
+    return np.array([[1, 0], [0, cis(np.pi / 4)]], dtype=np.complex128)
+
+
+def RX(theta):
+    """quantumflow/stdgates.py:179-205."""
+    c, s = np.cos(theta / 2), np.sin(theta / 2)
+    return np.array([[c, -1j * s], [-1j * s, c]], dtype=np.complex128)
+
+
+def RZ(theta):
+    """quantumflow/stdgates.py:236-262."""
+    return np.array([[cis(-theta / 2), 0], [0, cis(theta / 2)]], dtype=np.complex128)
+
+
+def ZZ(t):
+    """quantumflow/stdgates.py:944-968: diag(cis(-pi t/2), cis(pi t/2), cis(pi t/2), cis(-pi t/2))."""
+    th = np.pi * t
+    return np.diag([cis(-th / 2), cis(th / 2), cis(th / 2), cis(-th / 2)]).astype(np.complex128)
+
+
+def CZ():
+    """quantumflow/stdgates.py:267-288."""
+    return np.diag([1, 1, 1, -1]).astype(np.complex128)
+
+
+def CNOT():
+    """quantumflow/stdgates.py:291-312."""
+    return np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=np.complex128)
+
+
+# ------------------------------------------------------------- QAOA --------
+def qubo_ops(n, edges, p, beta, gamma, weights=None, node_weights=None):
+    """Gate list of quantumflow/qaoa.py:22-64 qubo_circuit for nodes 0..n-1:
+    H on every node; per step ZZ(-w*gamma/pi) per edge (given order),
+    RZ(node weight) where present (not gamma-scaled), RX(beta) per node."""
+    ops = [(H(), (q,)) for q in range(n)]
+    weights = [1.0] * len(edges) if weights is None else list(weights)
+    for s in range(p):
+        for (a, b), w in zip(edges, weights):
+            ops.append((ZZ(-w * gamma[s] / np.pi), (a, b)))
+        if node_weights is not None:
+            for q in range(n):
+                nw = node_weights[q]
+                if nw is not None and not (isinstance(nw, float) and np.isnan(nw)):
+                    ops.append((RZ(nw), (q,)))
+        for q in range(n):
+            ops.append((RX(beta[s]), (q,)))
+    return ops
+
+
+def graph_cuts(n, edges, weights=None):
+    """Cut value of every basis state, [2]*n float64.
+
+    Restates quantumflow/qaoa.py:68-81 (for each edge add its weight where the
+    two node bits differ), vectorised over all 2^n states; node q is axis q,
+    i.e. bit n-1-q of the flat index."""
+    x = np.arange(2 ** n, dtype=np.int64)
+    out = np.zeros(2 ** n, dtype=np.float64)
+    weights = [1.0] * len(edges) if weights is None else list(weights)
+    for (a, b), w in zip(edges, weights):
+        diff = ((x >> (n - 1 - a)) ^ (x >> (n - 1 - b))) & 1
+        out += w * diff
+    return out.reshape([2] * n)
+
+
+def qaoa_expectation(n, edges, p, beta, gamma, weights=None, node_weights=None):
+    """<C> of the QAOA state (examples/qaoa_maxcut.py:56-58 objective)."""
+    st = run_ops(zero_state(n), qubo_ops(n, edges, p, beta, gamma, weights, node_weights))
+    return expectation(st, graph_cuts(n, edges, weights))
+
+
+def qaoa_fd_gradient(n, edges, p, beta, gamma, h=1e-6, weights=None, node_weights=None):
+    """Central finite differences of <C> w.r.t. (gamma, beta); the gradient
+    oracle for the adjoint kernel (the reference differentiates only with its
+    TensorFlow backends, quantumflow/backend/tensorflowbk.py)."""
+    beta = np.array(beta, dtype=np.float64)
+    gamma = np.array(gamma, dtype=np.float64)
+    gg, gb = np.zeros(p), np.zeros(p)
+    for i in range(p):
+        for arr, dst in ((gamma, gg), (beta, gb)):
+            old = arr[i]
+            arr[i] = old + h
+            ep = qaoa_expectation(n, edges, p, beta, gamma, weights, node_weights)
+            arr[i] = old - h
+            em = qaoa_expectation(n, edges, p, beta, gamma, weights, node_weights)
+            arr[i] = old
+            dst[i] = (ep - em) / (2 * h)
+    return gg, gb
+
+
+# --------------------------------------------------- random-layer circuit --
+def cz_layer_ops(ops_array, umats):
+    """Decode the (kind, q0, q1) op table of the golden random-layer circuits
+    into (matrix, axes) pairs."""
+    out = []
+    for (kind, a, b), u in zip(ops_array, umats):
+        if kind == 1:
+            out.append((u, (int(a),)))
+        else:
+            out.append((CZ(), (int(a), int(b))))
+    return out

@@ -1,0 +1,130 @@
+"""Circuits (quantumflow/circuits.py:35-138).
+
+``Circuit.run`` hands the whole gate list to ``qf_run_circuit`` in one call;
+the native planner fuses consecutive gates into blocks and sweeps the state
+once per block instead of once per gate (the reference loops
+``ket = elem.run(ket)`` at quantumflow/circuits.py:97-98).
+"""
+from typing import Iterable, Iterator
+
+import numpy as np
+
+from . import _native as nat
+from . import config
+from .gates import identity_gate
+from .ops import Gate, Operation
+from .qubits import Qubits
+from .states import Buffer, State, compute_layout, zero_state
+
+__all__ = ["Circuit", "count_operations"]
+
+
+class Circuit(Operation):
+    """A sequence of operations (quantumflow/circuits.py:35-138)."""
+
+    def __init__(self, elements: Iterable[Operation] = None) -> None:
+        self.elements = list(elements) if elements is not None else []
+        self._pack_key = None
+        self._pack = None
+
+    def add(self, other: "Circuit") -> "Circuit":
+        return Circuit(self.elements + other.elements)
+
+    def extend(self, other: Operation) -> None:
+        if isinstance(other, Circuit):
+            self.elements.extend(other.elements)
+        else:
+            self.elements.append(other)
+
+    def __add__(self, other: "Circuit") -> "Circuit":
+        return self.add(other)
+
+    def __iadd__(self, other: Operation) -> "Circuit":
+        self.extend(other)
+        return self
+
+    def __iter__(self) -> Iterator[Operation]:
+        return self.elements.__iter__()
+
+    def size(self) -> int:
+        return len(self.elements)
+
+    @property
+    def qubits(self) -> Qubits:
+        """Sorted union of element qubits (quantumflow/circuits.py:75-85)."""
+        qbs = [q for elem in self.elements for q in elem.qubits]
+        return tuple(sorted(set(qbs)))
+
+    def gates(self):
+        """Flattened gate list (nested circuits expanded)."""
+        out = []
+        for e in self.elements:
+            if isinstance(e, Circuit):
+                out.extend(e.gates())
+            else:
+                out.append(e)
+        return out
+
+    def packed(self, qubits: Qubits):
+        """(op_k, op_axes, op_mats) arrays of the C ABI for a state on `qubits`."""
+        flat = self.gates()
+        key = (tuple(qubits), tuple(id(g) for g in flat))
+        if key == self._pack_key:
+            return self._pack
+        index = {q: i for i, q in enumerate(qubits)}
+        ks, axes, mats = [], [], []
+        for g in flat:
+            if not isinstance(g, Gate):
+                raise TypeError(f"{type(g).__name__} cannot run inside a fused circuit")
+            ks.append(g.qubit_nb)
+            axes.extend(index[q] for q in g.qubits)
+            mats.append(g.matrix_doubles())
+        op_k = np.asarray(ks, dtype=np.int32)
+        op_axes = np.asarray(axes, dtype=np.int32)
+        op_mats = np.ascontiguousarray(np.concatenate(mats) if mats else np.zeros(1))
+        self._pack_key, self._pack = key, (op_k, op_axes, op_mats, len(flat))
+        return self._pack
+
+    def run(self, ket: State = None, fusion_k: int = None) -> State:
+        """Apply the circuit (quantumflow/circuits.py:87-99); default initial
+        state |0...0> on the sorted circuit qubits."""
+        fusion_k = config.FUSION_K if fusion_k is None else fusion_k
+        fresh = ket is None
+        if fresh:
+            ket = zero_state(self.qubits)
+        flat = self.gates()
+        if any(not isinstance(g, Gate) for g in flat):
+            for elem in flat:  # mixed operations: run one at a time
+                ket = elem.run(ket)
+            return ket
+        op_k, op_axes, op_mats, nops = self.packed(ket.qubits)
+        src = ket.buffer.compute()
+        out = src if (fresh or src is not ket.buffer) else src.empty_like()
+        passes = (nat.ctypes.c_int * 1)()
+        nat.call("qf_run_circuit", nat.ptr(src.data), nat.ptr(out.data), src.n, src.layout, nops,
+                 op_k.ctypes.data_as(nat._ip), op_axes.ctypes.data_as(nat._ip),
+                 op_mats.ctypes.data_as(nat._dp), int(fusion_k), passes, nat.stream_handle(src.device))
+        self.last_passes = passes[0]
+        return State(out, ket.qubits, ket._memory)
+
+    def asgate(self) -> Gate:
+        gate = identity_gate(self.qubits)
+        for elem in self.elements:
+            gate = elem.asgate() @ gate
+        return gate
+
+    @property
+    def H(self) -> "Circuit":
+        """Reversed circuit of element inverses (quantumflow/circuits.py:128-133)."""
+        return Circuit([elem.H for elem in self.elements[::-1]])
+
+    def __str__(self) -> str:
+        return "\n".join(str(elem) for elem in self.elements)
+
+
+def count_operations(elements) -> dict:
+    """Count operation types (quantumflow/circuits.py count_operations)."""
+    out = {}
+    for e in elements:
+        out[type(e)] = out.get(type(e), 0) + 1
+    return out

@@ -1,0 +1,114 @@
+// Host+device interface of the gate engine shared by the .cu files.
+#pragma once
+#include <cstdint>
+#include <complex>
+#include <vector>
+#include <cuda_runtime.h>
+#include "qf_common.cuh"
+#include "qf_gb300.h"
+
+namespace qf {
+
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------- op classes ----
+enum OpType : uint8_t {
+  OP_DENSE1 = 1,  // 2x2 on one in-tile bit
+  OP_DENSE2 = 2,  // 4x4 on two in-tile bits
+  OP_DENSEK = 3,  // 2^k x 2^k (k = 3..5) on in-tile bits, warp per group
+  OP_MONO = 4,    // generalised permutation on k<=3 in-tile bits
+  OP_DIAG = 5,    // diagonal on k<=3 bits anywhere (elementwise)
+  OP_SIGN = 6,    // -1 where all k bits are set (CZ, CCZ); elementwise
+  OP_CUT = 7,     // psi_x *= table[cut[x]]  (QAOA cost layer); elementwise
+  OP_PHASE = 8,   // psi_x *= c (global scalar); elementwise
+};
+
+constexpr int TILE_MAX_OPS = 96;
+constexpr int TILE_MAX_COEF = 1152;
+constexpr int KMAX_DENSE = 5;
+
+struct TileOp {
+  uint8_t type;
+  uint8_t k;
+  uint8_t lb[5];    // local (tile) bit positions, matrix MSB first
+  uint8_t slb[5];   // the same, sorted ascending (group enumeration)
+  uint8_t gb[3];    // global bit positions (elementwise ops), MSB first
+  uint8_t perm[8];  // OP_MONO: source row for each output row
+  uint16_t coef;    // index of first coefficient
+  uint16_t ncoef;   // number of coefficients (OP_CUT: table size, index clamp)
+};
+
+struct TileParams {
+  const void* in;
+  void* out;
+  const uint16_t* cuts;  // OP_CUT source (device), may be null
+  int32_t n;             // qubits
+  int32_t L;             // contiguous low bits in a tile
+  int32_t nh;            // extra high tile bits
+  int32_t nops;
+  int32_t threads;
+  uint8_t hb[8];         // high tile bits (global positions), ascending
+  TileOp ops[TILE_MAX_OPS];
+  Coef coef[TILE_MAX_COEF];
+};
+
+// A host-side classified op (one gate).
+struct HostOp {
+  int k = 0;
+  int gb[KMAX_DENSE] = {0, 0, 0, 0, 0};  // global bit positions, matrix MSB first
+  uint8_t type = 0;
+  std::vector<cplx> m;        // dense: row-major 2^k x 2^k
+  std::vector<cplx> diag;     // OP_DIAG / OP_MONO phases (per output row)
+  int perm[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+  const uint16_t* cuts = nullptr;  // OP_CUT
+  std::vector<cplx> table;         // OP_CUT phase per cut value
+  cplx scalar{1.0, 0.0};           // OP_PHASE
+};
+
+// Fill one coefficient in the arithmetic of `layout`.
+inline Coef make_coef(cplx v, int layout) {
+  Coef c;
+  c.d[0] = 0.0;
+  c.d[1] = 0.0;
+  if (layout == C128) {
+    c.d[0] = v.real();
+    c.d[1] = v.imag();
+  } else if (layout == FF) {
+    float rh = static_cast<float>(v.real());
+    float rl = static_cast<float>(v.real() - static_cast<double>(rh));
+    float ih = static_cast<float>(v.imag());
+    float il = static_cast<float>(v.imag() - static_cast<double>(ih));
+    c.f[0] = rh;
+    c.f[1] = rl;
+    c.f[2] = ih;
+    c.f[3] = il;
+  } else {
+    c.f[0] = static_cast<float>(v.real());
+    c.f[1] = 0.f;
+    c.f[2] = static_cast<float>(v.imag());
+    c.f[3] = 0.f;
+  }
+  return c;
+}
+
+inline size_t elem_bytes(int layout) { return layout == C64 ? 8 : 16; }
+
+// Classify a k-qubit matrix into DIAG / SIGN / MONO / DENSE and fill HostOp.
+// Returns QF_OK or an error status.
+int classify_op(int k, const int* gbits, const double* mat_interleaved, HostOp& op);
+
+// Plan + launch a sequence of ops on one state (in -> out, may alias).
+int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
+            cudaStream_t stream, int* passes_out);
+
+// Launch helpers used by other translation units.
+int launch_tile_block(const void* in, void* out, int n, int layout, const std::vector<HostOp>& ops,
+                      const std::vector<int>& idx, uint64_t hmask, cudaStream_t stream);
+int launch_single(const void* in, void* out, int n, int layout, const HostOp& op, cudaStream_t stream);
+
+int device_sm_count();
+int timing_enable(int on);
+int timing_collect(double* ms, int64_t* counts, int nkinds);
+int check_cuda(cudaError_t e);
+
+}  // namespace qf

@@ -1,0 +1,277 @@
+// Shared device-side building blocks for the GB300 state-vector engine.
+//
+// State layout.  A state of n qubits is 2^n amplitudes in C order: flat index
+// x, with reference axis a stored at bit position (n-1-a) of x (axis 0 is the
+// most significant bit, quantumflow/qubits.py:63-69).  Three element layouts:
+//
+//   QF_LAYOUT_C64   complex64   float2  {re, im}                 8 B
+//   QF_LAYOUT_C128  complex128  double2 {re, im}                16 B
+//   QF_LAYOUT_FF    float-float float4  {re_hi, re_lo, im_hi, im_lo}  16 B
+//
+// FF carries a complex128 value as two unevaluated float sums
+// (value = hi + lo, |lo| <= ulp(hi)/2), a 48-bit significand.  GB300 issues
+// FP64 FMAs at ~1/64 of the FP32 rate, so a dense 2x2 complex gate in native
+// FP64 cannot keep up with HBM; the same gate in float-float arithmetic on
+// the FP32 pipes can.  Error-free transforms below (two_sum, two_prod) follow
+// Knuth (TAOCP vol. 2, 4.2.2) and Dekker (1971); the dot-product accumulation
+// is the compensated scheme of Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26 (2005).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define QF_HD __host__ __device__ __forceinline__
+#define QF_D __device__ __forceinline__
+
+namespace qf {
+
+enum Layout : int { C64 = 0, C128 = 1, FF = 2 };
+
+// ---------------------------------------------------------------- types ----
+template <int L> struct Types;
+template <> struct Types<C64>  { using E = float2;  };
+template <> struct Types<C128> { using E = double2; };
+template <> struct Types<FF>   { using E = float4;  };
+
+// A complex gate coefficient in the layout's arithmetic: for FF the four
+// floats are (re_hi, re_lo, im_hi, im_lo); for C64 only .x/.z are used
+// (re, im) and for C128 the double pair.  16 bytes in every case; the host
+// fills it for the layout of the kernel it launches (engine.cuh make_coef).
+struct Coef {
+  union {
+    double d[2];
+    float f[4];
+  };
+};
+
+// ---------------------------------------------------- error-free transforms
+QF_D void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+QF_D void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// Compensated accumulator for sums of float-float products.
+struct FFAcc {
+  float s, e;
+  QF_D void zero() { s = 0.f; e = 0.f; }
+  // += (ah + al) * (bh + bl); the al*bl term (2^-48 relative) is dropped.
+  QF_D void add_prod(float ah, float al, float bh, float bl) {
+    float p = __fmul_rn(ah, bh);
+    float pe = __fmaf_rn(ah, bh, -p);
+    float t;
+    two_sum(s, p, s, t);
+    float cross = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, pe));
+    e = __fadd_rn(e, __fadd_rn(t, cross));
+  }
+  QF_D void add(float h, float l) {
+    float t;
+    two_sum(s, h, s, t);
+    e = __fadd_rn(e, __fadd_rn(t, l));
+  }
+  QF_D void finish(float& hi, float& lo) const { fast_two_sum(s, e, hi, lo); }
+};
+
+// ---------------------------------------------------- complex dot products
+// out = sum_j u[j] * a[j] for J terms.  u comes from kernel parameters (warp
+// uniform), so the zero tests below are uniform branches: real or imaginary
+// coefficient parts that are exactly zero (RX, RZ, H, CNOT ...) cost nothing.
+template <int J>
+QF_D float2 cdot(const Coef* u, const float2* a) {
+  float re = 0.f, im = 0.f;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const float ur = u[j].f[0], ui = u[j].f[2];
+    re = fmaf(ur, a[j].x, re);
+    re = fmaf(-ui, a[j].y, re);
+    im = fmaf(ur, a[j].y, im);
+    im = fmaf(ui, a[j].x, im);
+  }
+  return make_float2(re, im);
+}
+
+template <int J>
+QF_D double2 cdot(const Coef* u, const double2* a) {
+  double re = 0.0, im = 0.0;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const double ur = u[j].d[0], ui = u[j].d[1];
+    if (ur != 0.0) {
+      re = fma(ur, a[j].x, re);
+      im = fma(ur, a[j].y, im);
+    }
+    if (ui != 0.0) {
+      re = fma(-ui, a[j].y, re);
+      im = fma(ui, a[j].x, im);
+    }
+  }
+  return make_double2(re, im);
+}
+
+template <int J>
+QF_D float4 cdot(const Coef* u, const float4* a) {
+  FFAcc re, im;
+  re.zero();
+  im.zero();
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const float urh = u[j].f[0], url = u[j].f[1], uih = u[j].f[2], uil = u[j].f[3];
+    if (urh != 0.f) {
+      re.add_prod(urh, url, a[j].x, a[j].y);
+      im.add_prod(urh, url, a[j].z, a[j].w);
+    }
+    if (uih != 0.f) {
+      re.add_prod(-uih, -uil, a[j].z, a[j].w);
+      im.add_prod(uih, uil, a[j].x, a[j].y);
+    }
+  }
+  float4 r;
+  re.finish(r.x, r.y);
+  im.finish(r.z, r.w);
+  return r;
+}
+
+// Per-thread (non-uniform) coefficient variants, no zero skipping.
+QF_D float2 cmul_add2(float2 u0, float2 a0, float2 u1, float2 a1) {
+  float re = u0.x * a0.x;
+  re = fmaf(-u0.y, a0.y, re);
+  re = fmaf(u1.x, a1.x, re);
+  re = fmaf(-u1.y, a1.y, re);
+  float im = u0.x * a0.y;
+  im = fmaf(u0.y, a0.x, im);
+  im = fmaf(u1.x, a1.y, im);
+  im = fmaf(u1.y, a1.x, im);
+  return make_float2(re, im);
+}
+QF_D double2 cmul_add2(double2 u0, double2 a0, double2 u1, double2 a1) {
+  double re = u0.x * a0.x;
+  re = fma(-u0.y, a0.y, re);
+  re = fma(u1.x, a1.x, re);
+  re = fma(-u1.y, a1.y, re);
+  double im = u0.x * a0.y;
+  im = fma(u0.y, a0.x, im);
+  im = fma(u1.x, a1.y, im);
+  im = fma(u1.y, a1.x, im);
+  return make_double2(re, im);
+}
+QF_D float4 cmul_add2(float4 u0, float4 a0, float4 u1, float4 a1) {
+  FFAcc re, im;
+  re.zero();
+  im.zero();
+  re.add_prod(u0.x, u0.y, a0.x, a0.y);
+  re.add_prod(-u0.z, -u0.w, a0.z, a0.w);
+  re.add_prod(u1.x, u1.y, a1.x, a1.y);
+  re.add_prod(-u1.z, -u1.w, a1.z, a1.w);
+  im.add_prod(u0.x, u0.y, a0.z, a0.w);
+  im.add_prod(u0.z, u0.w, a0.x, a0.y);
+  im.add_prod(u1.x, u1.y, a1.z, a1.w);
+  im.add_prod(u1.z, u1.w, a1.x, a1.y);
+  float4 r;
+  re.finish(r.x, r.y);
+  im.finish(r.z, r.w);
+  return r;
+}
+
+// single complex multiply by a uniform coefficient
+QF_D float2 cmul(const Coef& u, float2 a) { return cdot<1>(&u, &a); }
+QF_D double2 cmul(const Coef& u, double2 a) { return cdot<1>(&u, &a); }
+QF_D float4 cmul(const Coef& u, float4 a) { return cdot<1>(&u, &a); }
+
+QF_D float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
+QF_D double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+QF_D float4 cneg(float4 a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+
+// |a|^2 accumulated into a float-float accumulator (all layouts).
+QF_D void acc_norm2(FFAcc& acc, float2 a) {
+  acc.add_prod(a.x, 0.f, a.x, 0.f);
+  acc.add_prod(a.y, 0.f, a.y, 0.f);
+}
+QF_D void acc_norm2(FFAcc& acc, float4 a) {
+  acc.add_prod(a.x, a.y, a.x, a.y);
+  acc.add_prod(a.z, a.w, a.z, a.w);
+}
+// double amplitudes: split each component into float-float first
+QF_D void split_d(double d, float& h, float& l) {
+  h = __double2float_rn(d);
+  l = __double2float_rn(d - (double)h);
+}
+QF_D void acc_norm2(FFAcc& acc, double2 a) {
+  float rh, rl, ih, il;
+  split_d(a.x, rh, rl);
+  split_d(a.y, ih, il);
+  acc.add_prod(rh, rl, rh, rl);
+  acc.add_prod(ih, il, ih, il);
+}
+QF_D float4 to_ff(double2 a) {
+  float4 r;
+  split_d(a.x, r.x, r.y);
+  split_d(a.y, r.z, r.w);
+  return r;
+}
+QF_D float4 to_ff(float2 a) { return make_float4(a.x, 0.f, a.y, 0.f); }
+QF_D float4 to_ff(float4 a) { return a; }
+
+// ------------------------------------------------------------- indexing ----
+// Insert a zero bit at position b of v.
+QF_HD int64_t insert0(int64_t v, int b) {
+  const int64_t lo = v & ((int64_t(1) << b) - 1);
+  return ((v >> b) << (b + 1)) | lo;
+}
+
+// ---------------------------------------- mbarrier + bulk async copies -----
+QF_D uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+QF_D void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+QF_D void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+QF_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+QF_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared bulk copy completing on an mbarrier (16-byte aligned,
+// size a multiple of 16)
+QF_D void bulk_g2s(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(sdst)),
+      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// shared -> global bulk copy tracked in the issuing thread's bulk group
+QF_D void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(smem_u32(ssrc)), "r"(bytes)
+               : "memory");
+}
+QF_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+QF_D void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+QF_D void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+QF_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---------------------------------------------------- warp reductions ----
+QF_D double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace qf

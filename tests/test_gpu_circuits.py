@@ -1,0 +1,119 @@
+"""GPU parity: fused circuit execution against the reference's outputs, and
+size-independent properties at large N."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import qf_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _circuit_from_fixture(c, N):
+    import quantumflow_gb300 as qf
+    circ = qf.Circuit()
+    for (kind, a, b), u in zip(c[f"rc{N}_ops"], c[f"rc{N}_u"]):
+        circ += qf.Gate(u, qubits=[int(a)]) if kind == 1 else qf.CZ(int(a), int(b))
+    return circ
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-5)])
+@pytest.mark.parametrize("fusion_k", [1, 2, 4, 6, 8])
+def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k):
+    import quantumflow_gb300 as qf
+    c = golden["circuits"]
+    for N in (4, 6, 9, 12):
+        circ = _circuit_from_fixture(c, N)
+        ket = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k)
+        err = np.max(np.abs(ket.asarray().reshape(-1) - c[f"rc{N}_state"]))
+        assert err < tol, (N, err)
+        back = circ.H.run(ket, fusion_k=fusion_k)
+        err = np.max(np.abs(back.asarray().reshape(-1) - c[f"rc{N}_inverse"]))
+        assert err < tol * 2, (N, err)
+
+
+@pytest.mark.parametrize("arith", ["ff", "fp64"])
+def test_kat_circuits(golden, arith, monkeypatch):
+    import quantumflow_gb300 as qf
+    from math import pi
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", arith)
+    kat = golden["kat"]
+    circ = qf.Circuit()
+    circ += qf.RY(pi / 2, 0)
+    circ += qf.RX(pi, 0)
+    circ += qf.RY(pi / 2, 1)
+    circ += qf.RX(pi, 1)
+    circ += qf.CNOT(0, 1)
+    circ += qf.RX(-pi / 2, 1)
+    circ += qf.RY(4.71572463191, 1)
+    circ += qf.RX(pi / 2, 1)
+    circ += qf.CNOT(0, 1)
+    circ += qf.RX(-2 * 2.74973750579, 0)
+    circ += qf.RX(-2 * 2.74973750579, 1)
+    ket = circ.run(qf.zero_state(2))
+    np.testing.assert_allclose(ket.asarray().reshape(-1), kat["true_ket_ref_run"], atol=1e-13)
+    assert qf.states_close(ket, qf.State(kat["true_ket"].reshape(2, 2)))
+    # gates one at a time give the same state (Gate.run path)
+    k2 = qf.zero_state(2)
+    for g in circ:
+        k2 = g.run(k2)
+    np.testing.assert_allclose(k2.asarray(), ket.asarray(), atol=1e-14)
+
+
+def test_gops_circuit(golden):
+    import quantumflow_gb300 as qf
+    c = golden["circuits"]
+    circ = qf.Circuit([qf.H(n) for n in range(8)])
+    for q0, q1 in c["gops_pairs"]:
+        circ += qf.X(int(q0))
+        circ += qf.T(int(q1))
+        circ += qf.CNOT(int(q0), int(q1))
+    ket = circ.run(qf.zero_state(8))
+    assert np.max(np.abs(ket.asarray().reshape(-1) - c["gops_state"])) < 1e-12
+
+
+@pytest.mark.parametrize("N", [16, 22])
+def test_fused_equals_unfused_and_oracle(N):
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(N)
+    circ = qf.Circuit()
+    for layer in range(3):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    fused = circ.run(qf.zero_state(N), fusion_k=6)
+    unfused = circ.run(qf.zero_state(N), fusion_k=1)
+    assert circ.last_passes == len(circ.elements)
+    a, b = fused.asarray(), unfused.asarray()
+    assert np.max(np.abs(a - b)) < 1e-12
+    if N <= 16:
+        ops = [(g.asoperator(), tuple(g.qubits)) for g in circ]
+        ref = orc.run_ops(orc.zero_state(N), ops)
+        assert np.max(np.abs(a - ref)) < 1e-12
+
+
+@pytest.mark.parametrize("N", [26])
+def test_large_round_trip(N):
+    """Size-independent properties at large N: norm 1 after a random circuit,
+    and circuit.H restores |0...0> (complex128 and complex64)."""
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(7)
+    circ = qf.Circuit()
+    for q in range(N):
+        circ += qf.random_gate([q], random_state=rng)
+    for a in range(0, N - 1, 2):
+        circ += qf.CZ(a, a + 1)
+    for q in range(N):
+        circ += qf.random_gate([q], random_state=rng)
+    for dtype, tol in (("complex128", 1e-12), ("complex64", 2e-5)):
+        ket = circ.run(qf.zero_state(N, dtype=dtype))
+        assert abs(ket.norm() - 1) < tol * 10
+        back = circ.H.run(ket)
+        probs = back.probabilities()
+        assert abs(float(probs.reshape(-1)[0]) - 1) < tol * 10
+        del ket, back, probs
+        torch.cuda.empty_cache()

@@ -1,0 +1,97 @@
+"""GPU State operations: probabilities, norm, inner, expectation, sampling,
+measurement, constructors (quantumflow/states.py)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import qf_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def test_expectation_literals(golden):
+    # tests/test_gates.py:150-164 literals 42 and 2.5
+    import quantumflow_gb300 as qf
+    lit = golden["kat"]["expectation_literals"]
+    M = np.zeros([2] * 4)
+    M[0, 0, 0, 0] = 42
+    M[1, 0, 0, 0] = 1
+    M[0, 1, 0, 0] = 2
+    M[0, 0, 1, 0] = 3
+    M[0, 0, 0, 1] = 4
+    assert qf.zero_state(4).expectation(M) == lit[0]
+    assert abs(qf.w_state(4).expectation(M) - lit[1]) < 1e-14
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_reductions_against_oracle(dtype):
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(5)
+    tol = 1e-12 if dtype == "complex128" else 1e-6
+    for n in (1, 3, 10, 18):
+        a = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        b = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        sa, sb = qf.State(a, dtype=dtype), qf.State(b, dtype=dtype)
+        a_ = a.astype(np.complex64) if dtype == "complex64" else a
+        b_ = b.astype(np.complex64) if dtype == "complex64" else b
+        assert abs(sa.norm() - orc.norm(a_)) < tol * orc.norm(a_)
+        assert abs(qf.inner(sa, sb) - orc.inner(a_, b_)) < tol * 2 ** (n / 2) * 10
+        np.testing.assert_allclose(sa.probabilities().cpu().numpy().reshape(-1),
+                                   orc.probabilities(a_).reshape(-1), rtol=tol * 10, atol=0)
+        d = rng.normal(size=2 ** n)
+        assert abs(sa.expectation(d) - orc.expectation(a_, d)) < tol * 10 * orc.norm(a_)
+
+
+def test_ff_layout_reductions():
+    """Reductions read the float-float buffer directly (no conversion)."""
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(6)
+    n = 12
+    a = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    a /= np.linalg.norm(a)
+    st = qf.State(qf.Buffer.from_complex(torch.from_numpy(a).cuda()).to_layout(2))
+    assert abs(st.norm() - 1) < 1e-13
+    d = rng.uniform(size=2 ** n)
+    assert abs(st.expectation(d) - orc.expectation(a, d)) < 1e-13
+
+
+def test_sample_and_measure():
+    import quantumflow_gb300 as qf
+    ket = qf.zero_state(2)
+    ket = qf.H(0).run(ket)
+    ket = qf.CNOT(0, 1).run(ket)
+    counts = ket.sample(10)
+    assert counts.sum() == 10  # tests/test_states.py:124-130
+    assert counts[0, 1] == 0 and counts[1, 0] == 0
+    for _ in range(16):  # tests/test_states.py:108-121
+        res = ket.measure()
+        assert res[0] == res[1]
+    assert np.allclose(qf.zero_state(2).measure(), [0, 0])
+    assert np.allclose(qf.X(0).run(qf.zero_state(2)).measure(), [1, 0])
+    # statistics: 200k draws from a random 6-qubit state
+    rng = np.random.default_rng(8)
+    a = rng.normal(size=64) + 1j * rng.normal(size=64)
+    st = qf.State(a / np.linalg.norm(a))
+    trials = 200000
+    c = st.sample(trials, seed=1234).reshape(-1)
+    p = orc.probabilities(a / np.linalg.norm(a)).reshape(-1)
+    chi2 = np.sum((c - trials * p) ** 2 / (trials * p))
+    assert c.sum() == trials
+    assert chi2 < 150  # 63 degrees of freedom; p-value ~1e-8 at 150
+    ket = qf.H(0).run(qf.zero_state(1))
+    assert abs(ket.expectation([0.4, 0.6]) - 0.5) < 1e-12
+    assert abs(ket.expectation([0.4, 0.6], 4000) - 0.5) < 0.02
+
+
+def test_constructors_and_normalize():
+    import quantumflow_gb300 as qf
+    ghz = qf.ghz_state(3).asarray().reshape(-1)
+    assert abs(ghz[0] - 2 ** -0.5) < 1e-15 and abs(ghz[7] - 2 ** -0.5) < 1e-15
+    r = qf.random_state(5)
+    assert abs(r.norm() - 1) < 1e-13
+    u = qf.uniform_state(4).asarray().reshape(-1)
+    np.testing.assert_allclose(u, np.full(16, 0.25), atol=1e-15)
+    j = qf.join_states(qf.zero_state([0]), qf.X(1).run(qf.zero_state([1])))
+    assert j.qubits == (0, 1) and abs(j.asarray().reshape(-1)[1] - 1) < 1e-15
+    p = qf.State(np.arange(8)).permute([2, 1, 0]).asarray()
+    np.testing.assert_allclose(p, np.arange(8).reshape(2, 2, 2).transpose(2, 1, 0))

@@ -1,0 +1,84 @@
+"""The CPU oracle against the reference's own outputs (tests/golden, made by
+running the reference) and the literal known answers of its test suite."""
+import numpy as np
+import pytest
+
+from oracle import qf_oracle as orc
+
+
+def test_tensormul_matches_reference(golden):
+    g = golden["tensormul"]
+    for c in range(int(g["tm_count"])):
+        out = orc.tensormul(g[f"tm{c}_gate"], g[f"tm{c}_state"], list(g[f"tm{c}_idx"]))
+        np.testing.assert_allclose(out.reshape(-1), g[f"tm{c}_out"], rtol=0, atol=1e-12)
+
+
+def test_kat_true_ket():
+    # tests/test_circuits.py:43-60 circuit, KAT amplitudes from
+    # tests/test_circuits.py:19-24 (referenceQVM)
+    import quantumflow_gb300.stdgates as sg
+    from math import pi
+    ops = [(sg.RY(pi / 2).asoperator(), (0,)), (sg.RX(pi).asoperator(), (0,)),
+           (sg.RY(pi / 2).asoperator(), (1,)), (sg.RX(pi).asoperator(), (1,)),
+           (orc.CNOT(), (0, 1)), (sg.RX(-pi / 2).asoperator(), (1,)),
+           (sg.RY(4.71572463191).asoperator(), (1,)), (sg.RX(pi / 2).asoperator(), (1,)),
+           (orc.CNOT(), (0, 1)), (sg.RX(-2 * 2.74973750579).asoperator(), (0,)),
+           (sg.RX(-2 * 2.74973750579).asoperator(), (1,))]
+    from tests.conftest import load_golden
+    kat = load_golden("kat.npz")
+    st = orc.run_ops(orc.zero_state(2), ops).reshape(-1)
+    np.testing.assert_allclose(st, kat["true_ket_ref_run"], atol=1e-13)
+    # the literal KAT is printed to ~1e-8 precision
+    assert orc.fidelity(st, kat["true_ket"] / np.linalg.norm(kat["true_ket"])) > 1 - 1e-12
+
+
+def test_graph_cuts_literals(golden):
+    kat = golden["kat"]
+    # tests/test_qaoa.py:40-55
+    np.testing.assert_allclose(orc.graph_cuts(3, [(0, 1), (1, 2)]).reshape(-1), kat["cuts_unweighted"])
+    np.testing.assert_allclose(
+        orc.graph_cuts(3, [(0, 1), (1, 2), (0, 2)], [0.1, 0.4, 0.35]).reshape(-1), kat["cuts_weighted"])
+
+
+def test_qaoa_against_reference(golden):
+    q = golden["qaoa"]
+    for name in q["qaoa_cases"]:
+        n, p = int(q[f"{name}_n"]), int(q[f"{name}_p"])
+        edges = [tuple(e) for e in q[f"{name}_edges"]]
+        w = q[f"{name}_weights"]
+        nw = [None if np.isnan(v) else float(v) for v in q[f"{name}_node_weights"]]
+        beta, gamma = q[f"{name}_beta"], q[f"{name}_gamma"]
+        cuts = orc.graph_cuts(n, edges, w)
+        np.testing.assert_allclose(cuts.reshape(-1), q[f"{name}_cuts"], atol=1e-12)
+        st = orc.run_ops(orc.zero_state(n), orc.qubo_ops(n, edges, p, beta, gamma, w, nw))
+        np.testing.assert_allclose(st.reshape(-1), q[f"{name}_state"], atol=1e-12)
+        e = orc.expectation(st, cuts)
+        assert abs(e - float(q[f"{name}_expectation"])) < 1e-10
+        ops = orc.qubo_ops(n, edges, p, beta, gamma, w, nw)
+        assert len(ops) == int(q[f"{name}_nelements"])
+        if f"{name}_fd_grad_gamma" in q and n <= 8:
+            gg, gb = orc.qaoa_fd_gradient(n, edges, p, beta, gamma, 1e-6, w, nw)
+            np.testing.assert_allclose(gg, q[f"{name}_fd_grad_gamma"], atol=1e-6)
+            np.testing.assert_allclose(gb, q[f"{name}_fd_grad_beta"], atol=1e-6)
+
+
+def test_random_layer_circuits(golden):
+    c = golden["circuits"]
+    for N in (4, 6, 9, 12):
+        ops = orc.cz_layer_ops(c[f"rc{N}_ops"], c[f"rc{N}_u"])
+        st = orc.run_ops(orc.zero_state(N), ops).reshape(-1)
+        np.testing.assert_allclose(st, c[f"rc{N}_state"], atol=1e-12)
+
+
+def test_c1_gradient_ascent(golden):
+    # examples/qaoa_maxcut.py:37-87 semantics with FD gradients, lr 0.1, 5 steps
+    q = golden["qaoa"]
+    n, p = int(q["c1_n"]), int(q["c1_p"])
+    edges = [tuple(e) for e in q["c1_edges"]]
+    beta, gamma = q["c1_beta"].copy(), q["c1_gamma"].copy()
+    traj = []
+    for _ in range(5):
+        gg, gb = orc.qaoa_fd_gradient(n, edges, p, beta, gamma)
+        gamma, beta = gamma + 0.1 * gg, beta + 0.1 * gb
+        traj.append(orc.qaoa_expectation(n, edges, p, beta, gamma))
+    np.testing.assert_allclose(traj, q["c1_gd_expectations"], atol=1e-8)
