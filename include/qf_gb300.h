@@ -137,6 +137,20 @@ int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges
  * (quantumflow/states.py:131-147) with the diagonal of graph_cuts. */
 int qf_expectation_cuts(const void* psi, int n, int layout, const uint16_t* cuts, double* out,
                         void* workspace, size_t workspace_bytes, void* stream);
+/* Allocation-free variant of qf_expectation_cuts (same result, same
+ * arguments minus the workspace).  No counterpart in the reference.  It is
+ * for callers that cannot allocate or hand over device workspace -- e.g. a
+ * host whose memory pool owns the whole GPU, or a loop that must not call
+ * cudaMalloc because it can synchronise the device.  The partial sums live
+ * in a fixed array compiled into the library: QF_NOALLOC_MAX_PARTIALS block
+ * partials (32 KiB per GPU, held until exit), enough for every n up to
+ * QF_MAX_QUBITS (larger n: QF_ERR_TOO_LARGE).  All calls share that array,
+ * so calls whose kernels overlap on the GPU race; serialise them.  The first
+ * call on a device looks up the array's device address with that device
+ * current; make that call before any stream capture. */
+#define QF_NOALLOC_MAX_PARTIALS 2048
+int qf_expectation_cuts_noalloc(const void* psi, int n, int layout, const uint16_t* cuts, double* out,
+                                void* stream);
 /* out[0] = sum_x diag[x] |psi_x|^2 for a real device array diag[2^n]. */
 int qf_expectation_diag(const void* psi, int n, int layout, const double* diag, double* out,
                         void* workspace, size_t workspace_bytes, void* stream);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "qf_qaoa_state": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int, _vp]),
     "qf_expectation_cuts": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
+    "qf_expectation_cuts_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
     "qf_norm2": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _sz, _vp]),
     "qf_inner": (_c_int, [_vp, _vp, _c_int, _c_int, _vp, _vp, _sz, _vp]),
     "qf_probabilities": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
