@@ -188,8 +188,9 @@ def main():
     ap.add_argument("--layers", type=int, default=100)
     ap.add_argument("--dtype", default="complex128", choices=["complex128", "complex64"])
     ap.add_argument("--arith", default=None, choices=["ff", "fp64"])
-    ap.add_argument("--fusion", type=int, default=6)
+    ap.add_argument("--fusion", type=int, default=0, help="0 = library default per element type")
     ap.add_argument("--seed", type=int, default=2018)
+    ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-n", type=int, default=28)
@@ -219,6 +220,7 @@ def main():
     from quantumflow_gb300 import _native as nat
     if args.arith:
         qf.config.C128_ARITHMETIC = args.arith
+    nat.call("qf_set_tile_kernel", args.tile_mode)
 
     N, S = args.n, (16 if args.dtype == "complex128" else 8)
     sweep_bytes = 2 * S * 2 ** N
@@ -267,13 +269,12 @@ def main():
     launches = sum(c for _, c in kt.values()) + args.steps  # + one |0> fill per step
 
     peak, peak_kind = measured_peaks()
-    tile_ms, tile_n = kt["fused_tile"]
-    dom = "fused_tile" if tile_n else max(kt, key=lambda k: kt[k][0])
+    dom = max(kt, key=lambda k: kt[k][0])
     dom_ms, dom_n = kt[dom]
     achieved = sweep_bytes / (dom_ms / dom_n * 1e-3) / 1e9 if dom_n else None
     total_kernel_ms = sum(m for m, _ in kt.values())
     roofline = {
-        "bound": "hbm", "kernel": f"k_tile ({dom})", "achieved": achieved, "peak": peak,
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
         "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
         "traffic": None, "launches_timed": dom_n,
         "share_of_kernel_time": dom_ms / total_kernel_ms if total_kernel_ms else None,

@@ -77,8 +77,15 @@ size_t qf_reduce_workspace_bytes(int n);
 #define QF_KERNEL_DENSE2 2
 #define QF_KERNEL_PERMUTATION 3
 #define QF_KERNEL_ELEMENTWISE 4
-#define QF_KERNEL_CLASSES 5
+#define QF_KERNEL_WARP_TILE 5
+#define QF_KERNEL_CLASSES 6
 int qf_timing_enable(int on);
+/* Fused-pass kernel selection (diagnostics and tests; no reference
+ * counterpart), process-wide: 0 = default (warp tiles, then shared-memory
+ * register programs, then the shared-memory kernel, whichever first fits
+ * the block); 1 = shared-memory kernel only; 2, 3, 4 = default order with
+ * warp tiles of 2^mode registers per thread. */
+int qf_set_tile_kernel(int mode);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
 
 /* ------------------------------------------------- state preparation ------ */
@@ -127,6 +134,22 @@ int qf_cut_values_weighted(double* cuts, int n, int nedges, const int* edges, co
 int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p,
                   const double* beta, const double* gamma, const double* node_theta, int fusion_k,
                   void* stream);
+
+/* <C> and its gradient by the adjoint method: the forward state is built in
+ * psi (state-sized device buffer, left at |+>^n on return), lambda = C psi,
+ * then every layer is undone in reverse on both vectors while
+ *   d<C>/d beta_l  = sum_j Im <lambda|X_j|psi>          (after the mixer)
+ *   d<C>/d gamma_l = -2 Im <lambda|(E/2 - C)|psi>       (after the cost layer)
+ * accumulate.  Two state vectors regardless of p.  out (device, 2p+1
+ * doubles): out[0..p) = d/d gamma, out[p..2p) = d/d beta, out[2p] = <C>.
+ * Workspace: qf_qaoa_grad_workspace_bytes(n, p, layout), 256-byte aligned.
+ * The reference differentiates only through TensorFlow
+ * (examples/qaoa_maxcut.py:56-64, quantumflow/backend/tensorflowbk.py). */
+size_t qf_qaoa_grad_workspace_bytes(int n, int p, int layout);
+int qf_qaoa_expectation_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p,
+                             const double* beta, const double* gamma, const double* node_theta,
+                             int fusion_k, double* out, void* workspace, size_t workspace_bytes,
+                             void* stream);
 
 /* ------------------------------------------------------- reductions ------- */
 /* All reductions write their result to DEVICE memory `out` and need a

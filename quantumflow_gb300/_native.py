@@ -62,6 +62,7 @@ SIGNATURES = {
     "qf_get_device_error": (_c_int, [_ip, _vp]),
     "qf_reduce_workspace_bytes": (_sz, [_c_int]),
     "qf_timing_enable": (_c_int, [_c_int]),
+    "qf_set_tile_kernel": (_c_int, [_c_int]),
     "qf_timing_collect": (_c_int, [_dp, ctypes.POINTER(ctypes.c_int64), _c_int]),
     "qf_sample_workspace_bytes": (_sz, [_c_int]),
     "qf_fill_basis": (_c_int, [_vp, _c_int, _c_int, _c_i64, _vp]),
@@ -74,6 +75,9 @@ SIGNATURES = {
     "qf_cut_values_weighted": (_c_int, [_vp, _c_int, _c_int, _ip, _dp, _vp]),
     "qf_qaoa_state": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int, _vp]),
     "qf_expectation_cuts": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
+    "qf_qaoa_grad_workspace_bytes": (_sz, [_c_int, _c_int, _c_int]),
+    "qf_qaoa_expectation_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int,
+                                          _vp, _vp, _sz, _vp]),
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
     "qf_expectation_cuts_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
     "qf_norm2": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _sz, _vp]),
@@ -135,7 +139,7 @@ def device_error(stream=None):
     return flags.value
 
 
-KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise")
+KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile")
 
 
 def timing_enable(on=True):

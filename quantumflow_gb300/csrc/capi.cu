@@ -10,9 +10,14 @@
 
 namespace qf {
 extern thread_local int t_last_cuda_error;
+extern int g_force_smem_tile;
+extern int g_warp_rb_override;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
                const double* gamma, const double* node_theta, int fusion_k, cudaStream_t stream);
+size_t qaoa_grad_workspace_bytes(int n, int p, int layout);
+int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
+              const double* gamma, const double* node_theta, double* out, void* ws, cudaStream_t stream);
 }  // namespace qf
 
 using namespace qf;
@@ -77,6 +82,13 @@ int qf_last_cuda_error(void) { return t_last_cuda_error; }
 int qf_get_device_error(int* flags, void* stream) {
   if (flags == nullptr) return QF_ERR_INVALID_ARGUMENT;
   return read_clear_device_error(flags, as_stream(stream));
+}
+
+int qf_set_tile_kernel(int mode) {
+  if (mode < 0 || mode > 4) return QF_ERR_INVALID_ARGUMENT;
+  g_force_smem_tile = mode == 1;
+  g_warp_rb_override = mode >= 2 ? mode : 0;
+  return QF_OK;
 }
 
 int qf_timing_enable(int on) { return timing_enable(on); }
@@ -195,6 +207,29 @@ int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges
   if (nedges + 1 > 1024) return QF_ERR_TOO_LARGE;
   return qaoa_state(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, fusion_k,
                     as_stream(stream));
+}
+
+size_t qf_qaoa_grad_workspace_bytes(int n, int p, int layout) {
+  if (n < 1 || n > QF_MAX_QUBITS || p < 0 || !valid_layout(layout)) return 0;
+  return qaoa_grad_workspace_bytes(n, p, layout);
+}
+
+int qf_qaoa_expectation_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p,
+                             const double* beta, const double* gamma, const double* node_theta,
+                             int fusion_k, double* out, void* workspace, size_t workspace_bytes,
+                             void* stream) {
+  int rc = check_state(psi, n, layout);
+  if (rc) return rc;
+  if (cuts == nullptr || out == nullptr || p < 0 || nedges < 0) return QF_ERR_INVALID_ARGUMENT;
+  if (p > 0 && (beta == nullptr || gamma == nullptr)) return QF_ERR_INVALID_ARGUMENT;
+  if (nedges + 1 > 1024 || 2 * p + 1 > 64) return QF_ERR_TOO_LARGE;
+  rc = check_ws(workspace, workspace_bytes, qaoa_grad_workspace_bytes(n, p, layout));
+  if (rc) return rc;
+  if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
+  cudaStream_t s = as_stream(stream);
+  rc = qaoa_state(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, fusion_k, s);
+  if (rc) return rc;
+  return qaoa_grad(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, out, workspace, s);
 }
 
 int qf_expectation_cuts(const void* psi, int n, int layout, const uint16_t* cuts, double* out,

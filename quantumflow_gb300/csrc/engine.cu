@@ -292,116 +292,260 @@ QF_D int64_t global_of(const TileParams& P, int64_t base, int l) {
   return x;
 }
 
+// One op applied to a tile held in shared memory (all threads of the CTA;
+// the caller synchronises afterwards).
 template <int LAY>
-__device__ void tile_apply(const TileParams& P, typename Types<LAY>::E* s, int64_t base, int tbits) {
+__device__ void smem_op(const TileParams& P, const TileOp& op, const Coef* cf,
+                        typename Types<LAY>::E* s, int64_t base, int tbits) {
   using E = typename Types<LAY>::E;
   const int T = 1 << tbits;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+  switch (op.type) {
+    case OP_DENSE1: {
+      const int q = op.lb[0], bit = 1 << q;
+      for (int p = tid; p < (T >> 1); p += nthr) {
+        const int i0 = ins0(p, q);
+        E a[2] = {s[i0], s[i0 | bit]};
+        s[i0] = cdot<2>(cf, a);
+        s[i0 | bit] = cdot<2>(cf + 2, a);
+      }
+      break;
+    }
+    case OP_DENSE2: {
+      const int q0 = op.lb[0], q1 = op.lb[1];
+      const int lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0;
+      for (int p = tid; p < (T >> 2); p += nthr) {
+        const int b = ins0(ins0(p, lo), hi);
+        const int idx[4] = {b, b | (1 << q1), b | (1 << q0), b | (1 << q0) | (1 << q1)};
+        E a[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = s[idx[r]];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) s[idx[r]] = cdot<4>(cf + 4 * r, a);
+      }
+      break;
+    }
+    case OP_DENSEK: {
+      const int k = op.k, G = 1 << k;
+      for (int g = warp; g < (T >> k); g += nwarps) {
+        int b = g;
+        for (int i = 0; i < k; ++i) b = ins0(b, op.slb[i]);
+        E acc;
+        int mine = b;
+        if (lane < G) {
+          for (int i = 0; i < k; ++i)
+            if ((lane >> (k - 1 - i)) & 1) mine |= 1 << op.lb[i];
+          FFAcc ar, ai;  // accumulate in float-float for every layout
+          ar.zero();
+          ai.zero();
+          for (int j = 0; j < G; ++j) {
+            int src = b;
+            for (int i = 0; i < k; ++i)
+              if ((j >> (k - 1 - i)) & 1) src |= 1 << op.lb[i];
+            const float4 pf = to_ff(cmul_v(cf[lane * G + j], s[src]));
+            ar.add(pf.x, pf.y);
+            ai.add(pf.z, pf.w);
+          }
+          float rh, rl, ih, il;
+          ar.finish(rh, rl);
+          ai.finish(ih, il);
+          if constexpr (LAY == C64) {
+            acc = make_float2(rh + rl, ih + il);
+          } else if constexpr (LAY == C128) {
+            acc = make_double2((double)rh + (double)rl, (double)ih + (double)il);
+          } else {
+            acc = make_float4(rh, rl, ih, il);
+          }
+        }
+        __syncwarp();
+        if (lane < G) s[mine] = acc;
+        __syncwarp();
+      }
+      break;
+    }
+    case OP_MONO: {
+      const int k = op.k, G = 1 << k;
+      for (int g = tid; g < (T >> k); g += nthr) {
+        int b = g;
+        for (int i = 0; i < k; ++i) b = ins0(b, op.slb[i]);
+        int idx[8];
+        E a[8];
+        for (int r = 0; r < G; ++r) {
+          int x = b;
+          for (int i = 0; i < k; ++i)
+            if ((r >> (k - 1 - i)) & 1) x |= 1 << op.lb[i];
+          idx[r] = x;
+          a[r] = s[x];
+        }
+        for (int r = 0; r < G; ++r) s[idx[r]] = cmul(cf[r], a[op.perm[r]]);
+      }
+      break;
+    }
+    default: {  // element-wise ops
+      ElemOp eo;
+      eo.type = op.type;
+      eo.k = op.k;
+      eo.gb[0] = op.gb[0];
+      eo.gb[1] = op.gb[1];
+      eo.gb[2] = op.gb[2];
+      eo.coef = 0;
+      eo.ncoef = op.ncoef;
+      for (int l = tid; l < T; l += nthr) {
+        const int64_t x = global_of(P, base, l);
+        s[l] = elem_apply(eo, cf, P.cuts, x, s[l]);
+      }
+      break;
+    }
+  }
+}
+
+template <int LAY>
+__device__ void tile_apply(const TileParams& P, typename Types<LAY>::E* s, int64_t base, int tbits) {
   for (int o = 0; o < P.nops; ++o) {
     const TileOp& op = P.ops[o];
-    const Coef* cf = &P.coef[op.coef];
-    switch (op.type) {
-      case OP_DENSE1: {
-        const int q = op.lb[0], bit = 1 << q;
-        for (int p = tid; p < (T >> 1); p += nthr) {
-          const int i0 = ins0(p, q);
-          E a[2] = {s[i0], s[i0 | bit]};
-          s[i0] = cdot<2>(cf, a);
-          s[i0 | bit] = cdot<2>(cf + 2, a);
-        }
-        break;
-      }
-      case OP_DENSE2: {
-        const int q0 = op.lb[0], q1 = op.lb[1];
-        const int lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0;
-        for (int p = tid; p < (T >> 2); p += nthr) {
-          const int b = ins0(ins0(p, lo), hi);
-          const int idx[4] = {b, b | (1 << q1), b | (1 << q0), b | (1 << q0) | (1 << q1)};
-          E a[4];
+    smem_op<LAY>(P, op, &P.coef[op.coef], s, base, tbits);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------- register-resident programs ----
+template <int RB>
+QF_D int reg_local(const TMap& m, int r) {
+  int o = 0;
 #pragma unroll
-          for (int r = 0; r < 4; ++r) a[r] = s[idx[r]];
+  for (int j = 0; j < RB; ++j)
+    if ((r >> j) & 1) o |= 1 << m.rpos[j];
+  return o;
+}
+template <int RB>
+QF_D int64_t reg_global(const TMap& m, int r) {
+  int64_t o = 0;
 #pragma unroll
-          for (int r = 0; r < 4; ++r) s[idx[r]] = cdot<4>(cf + 4 * r, a);
+  for (int j = 0; j < RB; ++j)
+    if ((r >> j) & 1) o |= int64_t(1) << m.rglob[j];
+  return o;
+}
+QF_D int warp_local(const TMap& m, int warp) {
+  return (((warp >> 0) & 1) << m.wpos[0]) | (((warp >> 1) & 1) << m.wpos[1]) |
+         (((warp >> 2) & 1) << m.wpos[2]);
+}
+QF_D int64_t warp_global(const TMap& m, int warp) {
+  return (int64_t((warp >> 0) & 1) << m.wglob[0]) | (int64_t((warp >> 1) & 1) << m.wglob[1]) |
+         (int64_t((warp >> 2) & 1) << m.wglob[2]);
+}
+
+template <int RB, typename E>
+QF_D void regs_load(const E* s, const TMap& m, E (&a)[1 << RB], int lane, int warp) {
+  const int base = lane | warp_local(m, warp);
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) a[r] = s[base | reg_local<RB>(m, r)];
+}
+template <int RB, typename E>
+QF_D void regs_store(E* s, const TMap& m, const E (&a)[1 << RB], int lane, int warp) {
+  const int base = lane | warp_local(m, warp);
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) s[base | reg_local<RB>(m, r)] = a[r];
+}
+
+template <int RB, int J, typename E>
+QF_D void g1_reg(const Coef* cf, E (&a)[1 << RB]) {
+#pragma unroll
+  for (int i = 0; i < (1 << (RB - 1)); ++i) {
+    const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
+    const int i1 = i0 | (1 << J);
+    E p[2] = {a[i0], a[i1]};
+    a[i0] = cdot<2>(cf, p);
+    a[i1] = cdot<2>(cf + 2, p);
+  }
+}
+template <int RB, typename E>
+QF_D void g1_reg_dispatch(int j, const Coef* cf, E (&a)[1 << RB]) {
+  switch (j) {
+    case 0: g1_reg<RB, 0>(cf, a); break;
+    case 1: if constexpr (RB > 1) g1_reg<RB, 1>(cf, a); break;
+    case 2: if constexpr (RB > 2) g1_reg<RB, 2>(cf, a); break;
+    case 3: if constexpr (RB > 3) g1_reg<RB, 3>(cf, a); break;
+  }
+}
+
+template <int RB, int J0, int J1, typename E>
+QF_D void g2_reg(const Coef* cf, E (&a)[1 << RB]) {
+  constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
+#pragma unroll
+  for (int i = 0; i < (1 << (RB - 2)); ++i) {
+    int b = ((i >> LO) << (LO + 1)) | (i & ((1 << LO) - 1));
+    b = ((b >> HI) << (HI + 1)) | (b & ((1 << HI) - 1));
+    const int idx[4] = {b, b | (1 << J1), b | (1 << J0), b | (1 << J0) | (1 << J1)};
+    E p[4] = {a[idx[0]], a[idx[1]], a[idx[2]], a[idx[3]]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a[idx[r]] = cdot<4>(cf + 4 * r, p);
+  }
+}
+template <int RB, typename E>
+QF_D void g2_reg_dispatch(int j0, int j1, const Coef* cf, E (&a)[1 << RB]) {
+  switch (j0 * 4 + j1) {
+    case 1: g2_reg<RB, 0, 1>(cf, a); break;
+    case 4: g2_reg<RB, 1, 0>(cf, a); break;
+    case 2: if constexpr (RB > 2) g2_reg<RB, 0, 2>(cf, a); break;
+    case 8: if constexpr (RB > 2) g2_reg<RB, 2, 0>(cf, a); break;
+    case 6: if constexpr (RB > 2) g2_reg<RB, 1, 2>(cf, a); break;
+    case 9: if constexpr (RB > 2) g2_reg<RB, 2, 1>(cf, a); break;
+    case 3: if constexpr (RB > 3) g2_reg<RB, 0, 3>(cf, a); break;
+    case 12: if constexpr (RB > 3) g2_reg<RB, 3, 0>(cf, a); break;
+    case 7: if constexpr (RB > 3) g2_reg<RB, 1, 3>(cf, a); break;
+    case 13: if constexpr (RB > 3) g2_reg<RB, 3, 1>(cf, a); break;
+    case 11: if constexpr (RB > 3) g2_reg<RB, 2, 3>(cf, a); break;
+    case 14: if constexpr (RB > 3) g2_reg<RB, 3, 2>(cf, a); break;
+  }
+}
+
+template <int RB, typename E>
+QF_D void g1_lane(int l, const Coef* cf, E (&a)[1 << RB], int lane) {
+  const int hi = (lane >> l) & 1;
+  E* tag = nullptr;
+  const E cs = coef_e(cf[hi * 3], tag);
+  const E co = coef_e(cf[hi ? 2 : 1], tag);
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) {
+    const E p = shfl_xor(a[r], 1 << l);
+    a[r] = cmul_add2(cs, a[r], co, p);
+  }
+}
+
+// element-wise segment: x computed once per amplitude, sign ops folded into
+// one parity, phase ops multiplied in order
+template <int RB, typename E>
+QF_D void seg_apply(const TileParams& P, const TInstr& in, const TMap& m, const Coef* scoef,
+                    int64_t xbase, E (&a)[1 << RB]) {
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) {
+    const int64_t x = xbase | reg_global<RB>(m, r);
+    E v = a[r];
+    bool neg = false;
+    for (int o = in.a; o < in.a + in.b; ++o) {
+      const SegOp& so = P.segs[o];
+      switch (so.type) {
+        case OP_SIGN:
+          neg ^= ((uint64_t)x & so.mask) == so.mask;
+          break;
+        case OP_DIAG: {
+          int idx = 0;
+          for (int i = 0; i < so.k; ++i) idx = (idx << 1) | int((x >> so.gb[i]) & 1);
+          v = cmul_v(scoef[so.coef + idx], v);
+          break;
         }
-        break;
-      }
-      case OP_DENSEK: {
-        const int k = op.k, G = 1 << k;
-        E* tag = nullptr;
-        for (int g = warp; g < (T >> k); g += nwarps) {
-          int b = g;
-          for (int i = 0; i < k; ++i) b = ins0(b, op.slb[i]);
-          E acc;
-          int mine = b;
-          if (lane < G) {
-            for (int i = 0; i < k; ++i)
-              if ((lane >> (k - 1 - i)) & 1) mine |= 1 << op.lb[i];
-            FFAcc ar, ai;  // accumulate in float-float for every layout
-            ar.zero();
-            ai.zero();
-            for (int j = 0; j < G; ++j) {
-              int src = b;
-              for (int i = 0; i < k; ++i)
-                if ((j >> (k - 1 - i)) & 1) src |= 1 << op.lb[i];
-              const E prod = cmul_v(cf[lane * G + j], s[src]);
-              const float4 pf = to_ff(prod);
-              ar.add(pf.x, pf.y);
-              ai.add(pf.z, pf.w);
-            }
-            float rh, rl, ih, il;
-            ar.finish(rh, rl);
-            ai.finish(ih, il);
-            if constexpr (LAY == C64) {
-              acc = make_float2(rh + rl, ih + il);
-            } else if constexpr (LAY == C128) {
-              acc = make_double2((double)rh + (double)rl, (double)ih + (double)il);
-            } else {
-              acc = make_float4(rh, rl, ih, il);
-            }
-          }
-          (void)tag;
-          __syncwarp();
-          if (lane < G) s[mine] = acc;
-          __syncwarp();
+        case OP_CUT: {
+          const int c = min((int)P.cuts[x], so.ncoef - 1);
+          v = cmul_v(scoef[so.coef + c], v);
+          break;
         }
-        break;
-      }
-      case OP_MONO: {
-        const int k = op.k, G = 1 << k;
-        for (int g = tid; g < (T >> k); g += nthr) {
-          int b = g;
-          for (int i = 0; i < k; ++i) b = ins0(b, op.slb[i]);
-          int idx[8];
-          E a[8];
-          for (int r = 0; r < G; ++r) {
-            int x = b;
-            for (int i = 0; i < k; ++i)
-              if ((r >> (k - 1 - i)) & 1) x |= 1 << op.lb[i];
-            idx[r] = x;
-            a[r] = s[x];
-          }
-          for (int r = 0; r < G; ++r) s[idx[r]] = cmul(cf[r], a[op.perm[r]]);
-        }
-        break;
-      }
-      default: {  // element-wise ops
-        ElemOp eo;
-        eo.type = op.type;
-        eo.k = op.k;
-        eo.gb[0] = op.gb[0];
-        eo.gb[1] = op.gb[1];
-        eo.gb[2] = op.gb[2];
-        eo.coef = 0;
-        eo.ncoef = op.ncoef;
-        for (int l = tid; l < T; l += nthr) {
-          const int64_t x = global_of(P, base, l);
-          s[l] = elem_apply(eo, cf, P.cuts, x, s[l]);
-        }
-        break;
+        case OP_PHASE:
+          v = cmul_v(scoef[so.coef], v);
+          break;
       }
     }
-    __syncthreads();
+    a[r] = neg ? cneg(v) : v;
   }
 }
 
@@ -480,6 +624,199 @@ __global__ void __launch_bounds__(256) k_tile(const __grid_constant__ TileParams
     }
   }
   if (tid < 32) bulk_wait0();
+}
+
+template <int LAY, int RB>
+__global__ void __launch_bounds__(256) k_tile2(const __grid_constant__ TileParams P) {
+  using E = typename Types<LAY>::E;
+  constexpr int TBITS = RB + 8;
+  constexpr int T = 1 << TBITS;
+  // three tile buffers: while tile i is processed, tile i+1 streams in and
+  // tile i-1 streams out, so the prefetch never waits on a fresh store
+  constexpr int NST = 3;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[NST];
+  E* stage0 = reinterpret_cast<E*>(smem_raw);
+  Coef* scoef = reinterpret_cast<Coef*>(stage0 + NST * T);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t ntiles = int64_t(1) << (P.n - TBITS);
+  const uint32_t chunk_amps = 1u << P.L;
+  const uint32_t chunk_bytes = chunk_amps * (uint32_t)sizeof(E);
+  const int nchunks = 1 << P.nh;
+  const E* gin = reinterpret_cast<const E*>(P.in);
+  E* gout = reinterpret_cast<E*>(P.out);
+
+  for (int i = tid; i < P.necoef; i += blockDim.x) scoef[i] = P.coef[i];
+  if (tid == 0) {
+    for (int i = 0; i < NST; ++i) mbar_init(&bars[i], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto issue_load = [&](int64_t t, int s) {  // all 32 lanes of warp 0
+    if (lane == 0) mbar_arrive_expect_tx(&bars[s], (uint32_t)T * (uint32_t)sizeof(E));
+    __syncwarp();
+    const int64_t base = tile_base_of(P, t);
+    E* dst = stage0 + (size_t)s * T;
+    for (int c = lane; c < nchunks; c += 32)
+      bulk_g2s(dst + (size_t)c * chunk_amps, gin + base + chunk_off_of(P, c), chunk_bytes, &bars[s]);
+  };
+
+  E a[1 << RB];
+  int64_t t = blockIdx.x;
+  if (tid < 32 && t < ntiles) issue_load(t, 0);
+  uint32_t it = 0;
+  for (; t < ntiles; t += gridDim.x, ++it) {
+    const int s = it % NST;
+    const int64_t nxt = t + gridDim.x;
+    if (tid < 32 && nxt < ntiles) {
+      // the next load reuses the buffer of tile it-2: its store (the older
+      // of the two pending groups) must have finished reading
+      bulk_wait_read1();
+      __syncwarp();
+      issue_load(nxt, (it + 1) % NST);
+    }
+    const bool ok = mbar_wait_timed(&bars[s], (it / NST) & 1);
+    if (__syncthreads_or(!ok)) break;
+    E* st = stage0 + (size_t)s * T;
+    const int64_t base = tile_base_of(P, t);
+    int map = 0;
+    int64_t xbase = 0;
+    for (int pc = 0; pc < P.nprog; ++pc) {
+      const TInstr in = P.prog[pc];
+      switch (in.code) {
+        case I_MAP: {
+          if (pc > 0) {
+            regs_store<RB>(st, P.maps[map], a, lane, warp);
+            __syncthreads();
+          }
+          map = in.a;
+          regs_load<RB>(st, P.maps[map], a, lane, warp);
+          __syncthreads();
+          xbase = base | lane | warp_global(P.maps[map], warp);
+          break;
+        }
+        case I_G1R:
+          g1_reg_dispatch<RB>(in.a, &P.coef[in.coef], a);
+          break;
+        case I_G1L:
+          g1_lane<RB>(in.a, &P.coef[in.coef], a, lane);
+          break;
+        case I_G2R:
+          g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
+          break;
+        case I_SEG:
+          seg_apply<RB>(P, in, P.maps[map], scoef, xbase, a);
+          break;
+        case I_SMEM: {
+          regs_store<RB>(st, P.maps[map], a, lane, warp);
+          __syncthreads();
+          const TileOp& op = P.ops[in.a];
+          smem_op<LAY>(P, op, &P.coef[op.coef], st, base, TBITS);
+          __syncthreads();
+          regs_load<RB>(st, P.maps[map], a, lane, warp);
+          __syncthreads();
+          break;
+        }
+      }
+    }
+    regs_store<RB>(st, P.maps[map], a, lane, warp);
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid < 32) {
+      for (int c = lane; c < nchunks; c += 32)
+        bulk_s2g(gout + base + chunk_off_of(P, c), st + (size_t)c * chunk_amps, chunk_bytes);
+      bulk_commit();
+    }
+  }
+  if (tid < 32) bulk_wait0();
+}
+
+// -------------------------------------------------------------- k_warp ----
+template <int RB, typename E>
+QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t xb,
+                      const int64_t (&hoff)[1 << RB], E (&a)[1 << RB]) {
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) {
+    const int64_t x = xb | hoff[r];
+    E v = a[r];
+    bool neg = false;
+    for (int o = in.a; o < in.a + in.b; ++o) {
+      const SegOp& so = P.segs[o];
+      switch (so.type) {
+        case OP_SIGN:
+          neg ^= ((uint64_t)x & so.mask) == so.mask;
+          break;
+        case OP_DIAG: {
+          int idx = 0;
+          for (int i = 0; i < so.k; ++i) idx = (idx << 1) | int((x >> so.gb[i]) & 1);
+          v = cmul_v(scoef[so.coef + idx], v);
+          break;
+        }
+        case OP_CUT: {
+          const int c = min((int)P.cuts[x], so.ncoef - 1);
+          v = cmul_v(scoef[so.coef + c], v);
+          break;
+        }
+        case OP_PHASE:
+          v = cmul_v(scoef[so.coef], v);
+          break;
+      }
+    }
+    a[r] = neg ? cneg(v) : v;
+  }
+}
+
+template <int LAY, int RB>
+__global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams P) {
+  using E = typename Types<LAY>::E;
+  constexpr int R = 1 << RB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Coef* scoef = reinterpret_cast<Coef*>(smem_raw);
+  for (int i = threadIdx.x; i < P.necoef; i += blockDim.x) scoef[i] = P.coef[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t nsub = int64_t(1) << (P.n - 5 - RB);
+  const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+  int64_t hoff[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    int64_t o = 0;
+#pragma unroll
+    for (int j = 0; j < RB; ++j)
+      if ((r >> j) & 1) o |= int64_t(1) << P.hb[j];
+    hoff[r] = o;
+  }
+  const E* gin = reinterpret_cast<const E*>(P.in);
+  E* gout = reinterpret_cast<E*>(P.out);
+  for (int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); st < nsub; st += wstride) {
+    int64_t base = st << 5;
+#pragma unroll
+    for (int j = 0; j < RB; ++j) base = insert0(base, P.hb[j]);
+    const int64_t xb = base | lane;
+    E a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r] = gin[xb | hoff[r]];
+    for (int pc = 0; pc < P.nprog; ++pc) {
+      const TInstr in = P.prog[pc];
+      switch (in.code) {
+        case I_G1R:
+          g1_reg_dispatch<RB>(in.a, &P.coef[in.coef], a);
+          break;
+        case I_G1L:
+          g1_lane<RB>(in.a, &P.coef[in.coef], a, lane);
+          break;
+        case I_G2R:
+          g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
+          break;
+        case I_SEG:
+          seg_apply_w<RB>(P, in, scoef, xb, hoff, a);
+          break;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) gout[xb | hoff[r]] = a[r];
+  }
 }
 
 // ============================================================== host side
@@ -769,11 +1106,146 @@ static void tile_geometry(int n, int layout, uint64_t hmask, int& L, int& nh, ui
     if ((hmask >> b) & 1) hb[nh++] = (uint8_t)b;
 }
 
+// Compile a fused block into a k_tile2 register program.  Returns false
+// when the block does not fit the register scheme (the shared-memory kernel
+// k_tile then runs it).
+static bool compile_program(TileParams& P, const std::vector<HostOp>& ops, const std::vector<int>& idx,
+                            const std::vector<int>& local_bits_flat, int RB) {
+  const int tb = P.L + P.nh;
+  if (tb != RB + 8) return false;
+  auto gpos = [&](int lb) -> int { return lb < P.L ? lb : P.hb[lb - P.L]; };
+  const int nop = (int)idx.size();
+  std::vector<TInstr> prog;
+  std::vector<TMap> maps;
+  std::vector<SegOp> segs;
+  std::vector<int> regset;  // local bits held in registers (size RB) under the current map
+  auto lb_of = [&](int i, int j) { return local_bits_flat[i * KMAX_DENSE + j]; };
+
+  auto lookahead = [&](int from, std::vector<int> must) {
+    std::vector<int> set = must;
+    auto add = [&](int b) {
+      if ((int)set.size() < RB && b >= 5 && std::find(set.begin(), set.end(), b) == set.end()) set.push_back(b);
+    };
+    for (int i = from; i < nop && (int)set.size() < RB; ++i) {
+      const HostOp& op = ops[idx[i]];
+      if (op.type == OP_DENSE1) add(lb_of(i, 0));
+      if (op.type == OP_DENSE2 && lb_of(i, 0) >= 5 && lb_of(i, 1) >= 5 && (int)set.size() + 2 <= RB) {
+        add(lb_of(i, 0));
+        add(lb_of(i, 1));
+      }
+    }
+    for (int b = 5; b < tb && (int)set.size() < RB; ++b) add(b);
+    return set;
+  };
+  auto emit_map = [&](const std::vector<int>& set) -> bool {
+    if ((int)maps.size() >= TILE_MAX_MAPS) return false;
+    TMap m;
+    std::memset(&m, 0, sizeof(m));
+    int w = 0;
+    for (int j = 0; j < RB; ++j) {
+      m.rpos[j] = (uint8_t)set[j];
+      m.rglob[j] = (uint8_t)gpos(set[j]);
+    }
+    for (int b = 5; b < tb; ++b)
+      if (std::find(set.begin(), set.end(), b) == set.end()) {
+        if (w >= 3) return false;
+        m.wpos[w] = (uint8_t)b;
+        m.wglob[w] = (uint8_t)gpos(b);
+        ++w;
+      }
+    if (w != 3) return false;
+    maps.push_back(m);
+    TInstr in{I_MAP, (uint8_t)(maps.size() - 1), 0, 0, 0, 0};
+    prog.push_back(in);
+    regset = set;
+    return true;
+  };
+  auto ensure_map = [&](int from) -> bool {
+    if (!regset.empty()) return true;
+    return emit_map(lookahead(from, {}));
+  };
+  auto reg_index = [&](int b) -> int {
+    for (int j = 0; j < (int)regset.size(); ++j)
+      if (regset[j] == b) return j;
+    return -1;
+  };
+  for (int i = 0; i < nop; ++i) {
+    const HostOp& op = ops[idx[i]];
+    const TileOp& top = P.ops[i];
+    if (is_elementwise(op.type)) {
+      if (!ensure_map(i)) return false;
+      if ((int)segs.size() >= TILE_MAX_SEGS) return false;
+      SegOp so;
+      std::memset(&so, 0, sizeof(so));
+      so.type = op.type;
+      so.k = (uint8_t)op.k;
+      for (int j = 0; j < op.k && j < 3; ++j) {
+        so.gb[j] = (uint8_t)op.gb[j];
+        so.mask |= uint64_t(1) << op.gb[j];
+      }
+      so.coef = top.coef;
+      so.ncoef = top.ncoef;
+      segs.push_back(so);
+      if (!prog.empty() && prog.back().code == I_SEG && prog.back().a + prog.back().b == (int)segs.size() - 1 &&
+          prog.back().b < 255) {
+        prog.back().b++;
+      } else {
+        TInstr in{I_SEG, (uint8_t)(segs.size() - 1), 1, 0, 0, 0};
+        prog.push_back(in);
+      }
+      continue;
+    }
+    if (op.type == OP_DENSE1) {
+      const int q = lb_of(i, 0);
+      if (q < 5) {
+        if (!ensure_map(i)) return false;
+        prog.push_back(TInstr{I_G1L, (uint8_t)q, 0, 0, top.coef, 0});
+        continue;
+      }
+      if (reg_index(q) < 0 && !emit_map(lookahead(i, {q}))) return false;
+      prog.push_back(TInstr{I_G1R, (uint8_t)reg_index(q), 0, 0, top.coef, 0});
+      continue;
+    }
+    if (op.type == OP_DENSE2 && lb_of(i, 0) >= 5 && lb_of(i, 1) >= 5) {
+      const int q0 = lb_of(i, 0), q1 = lb_of(i, 1);
+      if (reg_index(q0) < 0 || reg_index(q1) < 0) {
+        if (!emit_map(lookahead(i, {q0, q1}))) return false;
+      }
+      prog.push_back(TInstr{I_G2R, (uint8_t)reg_index(q0), (uint8_t)reg_index(q1), 0, top.coef, 0});
+      continue;
+    }
+    if (!ensure_map(i)) return false;
+    prog.push_back(TInstr{I_SMEM, (uint8_t)i, 0, 0, 0, 0});
+  }
+  if ((int)prog.size() > TILE_MAX_PROG) return false;
+  P.nprog = (int)prog.size();
+  std::copy(prog.begin(), prog.end(), P.prog);
+  std::copy(maps.begin(), maps.end(), P.maps);
+  std::copy(segs.begin(), segs.end(), P.segs);
+  return true;
+}
+
+template <typename K>
+static int set_smem_attr(K kernel, std::atomic<bool>* flags) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !flags[dev].load()) {
+    int rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    if (rc) return rc;
+    flags[dev].store(true);
+  }
+  return QF_OK;
+}
+
+int g_force_smem_tile = 0;    // qf_set_tile_kernel: 1 = shared-memory tile kernels only
+int g_warp_rb_override = 0;  // qf_set_tile_kernel: register bits of k_warp (0 = per layout)
+
 template <int LAY>
 static int launch_tile_t(const void* in, void* out, int n, const std::vector<HostOp>& ops,
                          const std::vector<int>& idx, uint64_t hmask, cudaStream_t stream) {
   using E = typename Types<LAY>::E;
-  static thread_local TileParams P;  // ~20 KiB: kept off the stack
+  constexpr int RB = LAY == C64 ? 4 : 3;
+  static thread_local TileParams P;  // ~25 KiB: kept off the stack
   std::memset(&P, 0, sizeof(TileParams));
   P.in = in;
   P.out = out;
@@ -789,75 +1261,214 @@ static int launch_tile_t(const void* in, void* out, int n, const std::vector<Hos
       if (P.hb[r] == b) return L + r;
     return -1;
   };
+  if ((int)idx.size() > TILE_MAX_OPS) return QF_ERR_TOO_LARGE;
+  std::vector<int> local_bits(idx.size() * KMAX_DENSE, -1);
+  // coefficients: element-wise ops first (k_tile2 stages them in shared
+  // memory), then the rest
   int nc = 0;
-  P.nops = 0;
-  for (int i : idx) {
-    const HostOp& op = ops[i];
-    if (P.nops >= TILE_MAX_OPS) return QF_ERR_TOO_LARGE;
-    TileOp& t = P.ops[P.nops++];
-    t.type = op.type;
-    t.k = (uint8_t)op.k;
-    t.coef = (uint16_t)nc;
-    t.ncoef = (uint16_t)coef_count(op);
-    if (!is_elementwise(op.type)) {
-      int sl[KMAX_DENSE];
-      for (int j = 0; j < op.k; ++j) {
-        const int lb = local_of(op.gb[j]);
-        if (lb < 0) return QF_ERR_INVALID_ARGUMENT;
-        t.lb[j] = (uint8_t)lb;
-        sl[j] = lb;
-      }
-      std::sort(sl, sl + op.k);
-      for (int j = 0; j < op.k; ++j) t.slb[j] = (uint8_t)sl[j];
-    } else {
-      for (int j = 0; j < op.k && j < 3; ++j) t.gb[j] = (uint8_t)op.gb[j];
-    }
-    const int need = coef_count(op);
-    if (nc + need > TILE_MAX_COEF) return QF_ERR_TOO_LARGE;
-    switch (op.type) {
-      case OP_DENSE1:
-      case OP_DENSE2:
-      case OP_DENSEK:
-        for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.m[r], LAY);
-        break;
-      case OP_MONO:
-        for (int r = 0; r < need; ++r) {
-          P.coef[nc + r] = make_coef(op.diag[r], LAY);
-          t.perm[r] = (uint8_t)op.perm[r];
+  for (int pass = 0; pass < 2; ++pass) {
+    for (size_t i = 0; i < idx.size(); ++i) {
+      const HostOp& op = ops[idx[i]];
+      if (is_elementwise(op.type) != (pass == 0)) continue;
+      TileOp& t = P.ops[i];
+      t.type = op.type;
+      t.k = (uint8_t)op.k;
+      t.coef = (uint16_t)nc;
+      t.ncoef = (uint16_t)coef_count(op);
+      if (!is_elementwise(op.type)) {
+        int sl[KMAX_DENSE];
+        for (int j = 0; j < op.k; ++j) {
+          const int lb = local_of(op.gb[j]);
+          if (lb < 0) return QF_ERR_INVALID_ARGUMENT;
+          t.lb[j] = (uint8_t)lb;
+          sl[j] = lb;
+          local_bits[i * KMAX_DENSE + j] = lb;
         }
-        break;
-      case OP_DIAG:
-        for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.diag[r], LAY);
-        break;
-      case OP_CUT:
-        for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.table[r], LAY);
-        P.cuts = op.cuts;
-        break;
-      case OP_PHASE:
-        P.coef[nc] = make_coef(op.scalar, LAY);
-        break;
-      default:
-        break;
+        std::sort(sl, sl + op.k);
+        for (int j = 0; j < op.k; ++j) t.slb[j] = (uint8_t)sl[j];
+      } else {
+        for (int j = 0; j < op.k && j < 3; ++j) t.gb[j] = (uint8_t)op.gb[j];
+      }
+      const int need = coef_count(op);
+      if (nc + need > TILE_MAX_COEF) return QF_ERR_TOO_LARGE;
+      switch (op.type) {
+        case OP_DENSE1:
+        case OP_DENSE2:
+        case OP_DENSEK:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.m[r], LAY);
+          break;
+        case OP_MONO:
+          for (int r = 0; r < need; ++r) {
+            P.coef[nc + r] = make_coef(op.diag[r], LAY);
+            t.perm[r] = (uint8_t)op.perm[r];
+          }
+          break;
+        case OP_DIAG:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.diag[r], LAY);
+          break;
+        case OP_CUT:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.table[r], LAY);
+          P.cuts = op.cuts;
+          break;
+        case OP_PHASE:
+          P.coef[nc] = make_coef(op.scalar, LAY);
+          break;
+        default:
+          break;
+      }
+      nc += need;
     }
-    nc += need;
+    if (pass == 0) P.necoef = nc;
   }
+  P.nops = (int)idx.size();
+  P.threads = 256;
   const int tbits = L + nh;
-  const size_t smem = 2 * (size_t(1) << tbits) * sizeof(E);
-  static std::atomic<bool> attr_set[64];
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !attr_set[dev].load()) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_tile<LAY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             200 * 1024));
-    if (rc) return rc;
-    attr_set[dev].store(true);
-  }
   const int64_t ntiles = int64_t(1) << (n - tbits);
+  static std::atomic<bool> attr1[64], attr2[64];
+  if (!g_force_smem_tile && compile_program(P, ops, idx, local_bits, RB)) {
+    const size_t smem = 3 * (size_t(1) << tbits) * sizeof(E) + (size_t)P.necoef * sizeof(Coef);
+    if (smem <= 200 * 1024) {
+      int rc = set_smem_attr(k_tile2<LAY, RB>, attr2);
+      if (rc) return rc;
+      int64_t grid = (int64_t)device_sm_count() * 2;
+      if (grid > ntiles) grid = ntiles;
+      k_tile2<LAY, RB><<<(int)grid, 256, smem, stream>>>(P);
+      return check_cuda(cudaGetLastError());
+    }
+  }
+  P.nprog = 0;
+  const size_t smem = 2 * (size_t(1) << tbits) * sizeof(E);
+  int rc = set_smem_attr(k_tile<LAY>, attr1);
+  if (rc) return rc;
   int64_t grid = (int64_t)device_sm_count() * (smem > 80 * 1024 ? 2 : 3);
   if (grid > ntiles) grid = ntiles;
-  P.threads = 256;
   k_tile<LAY><<<(int)grid, 256, smem, stream>>>(P);
   return check_cuda(cudaGetLastError());
+}
+
+// Compile and launch a block on k_warp.  Returns QF_ERR_NOT_SUPPORTED (and
+// launches nothing) when the block does not fit the warp-tile scheme.
+template <int LAY, int RB>
+static int launch_warp_t(const void* in, void* out, int n, const std::vector<HostOp>& ops,
+                         const std::vector<int>& idx, cudaStream_t stream) {
+  using E = typename Types<LAY>::E;
+  if (n < 5 + RB) return QF_ERR_NOT_SUPPORTED;
+  static thread_local WarpParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.in = in;
+  P.out = out;
+  P.n = n;
+  P.rb = RB;
+  // register bits: the block's high bits, padded with unused bits >= 5
+  std::vector<int> hb;
+  for (int i : idx) {
+    const HostOp& op = ops[i];
+    if (is_elementwise(op.type)) continue;
+    if (op.type != OP_DENSE1 && op.type != OP_DENSE2) return QF_ERR_NOT_SUPPORTED;
+    for (int j = 0; j < op.k; ++j)
+      if (op.gb[j] >= 5 && std::find(hb.begin(), hb.end(), op.gb[j]) == hb.end()) hb.push_back(op.gb[j]);
+    if (op.type == OP_DENSE2 && (op.gb[0] < 5 || op.gb[1] < 5)) return QF_ERR_NOT_SUPPORTED;
+  }
+  if ((int)hb.size() > RB) return QF_ERR_NOT_SUPPORTED;
+  for (int b = 5; b < n && (int)hb.size() < RB; ++b)
+    if (std::find(hb.begin(), hb.end(), b) == hb.end()) hb.push_back(b);
+  std::sort(hb.begin(), hb.end());
+  for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];
+  auto reg_of = [&](int b) { return (int)(std::find(hb.begin(), hb.end(), b) - hb.begin()); };
+  // element-wise coefficients first (staged in shared memory), then dense
+  int nc = 0, nprog = 0, nseg = 0;
+  std::vector<int> coef_at(idx.size(), 0);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (size_t i = 0; i < idx.size(); ++i) {
+      const HostOp& op = ops[idx[i]];
+      if (is_elementwise(op.type) != (pass == 0)) continue;
+      const int need = coef_count(op);
+      if (nc + need > 1152) return QF_ERR_NOT_SUPPORTED;
+      coef_at[i] = nc;
+      switch (op.type) {
+        case OP_DENSE1:
+        case OP_DENSE2:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.m[r], LAY);
+          break;
+        case OP_DIAG:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.diag[r], LAY);
+          break;
+        case OP_CUT:
+          for (int r = 0; r < need; ++r) P.coef[nc + r] = make_coef(op.table[r], LAY);
+          P.cuts = op.cuts;
+          break;
+        case OP_PHASE:
+          P.coef[nc] = make_coef(op.scalar, LAY);
+          break;
+        default:
+          break;
+      }
+      nc += need;
+    }
+    if (pass == 0) P.necoef = nc;
+  }
+  for (size_t i = 0; i < idx.size(); ++i) {
+    const HostOp& op = ops[idx[i]];
+    if (nprog >= 160) return QF_ERR_NOT_SUPPORTED;
+    if (is_elementwise(op.type)) {
+      if (nseg >= 64) return QF_ERR_NOT_SUPPORTED;
+      SegOp& so = P.segs[nseg];
+      std::memset(&so, 0, sizeof(so));
+      so.type = op.type;
+      so.k = (uint8_t)op.k;
+      for (int j = 0; j < op.k && j < 3; ++j) {
+        so.gb[j] = (uint8_t)op.gb[j];
+        so.mask |= uint64_t(1) << op.gb[j];
+      }
+      so.coef = (uint16_t)coef_at[i];
+      so.ncoef = (uint16_t)coef_count(op);
+      if (nprog > 0 && P.prog[nprog - 1].code == I_SEG && P.prog[nprog - 1].b < 255 &&
+          P.prog[nprog - 1].a + P.prog[nprog - 1].b == nseg) {
+        P.prog[nprog - 1].b++;
+      } else {
+        P.prog[nprog++] = TInstr{I_SEG, (uint8_t)nseg, 1, 0, 0, 0};
+      }
+      ++nseg;
+    } else if (op.type == OP_DENSE1) {
+      const int b = op.gb[0];
+      if (b < 5) P.prog[nprog++] = TInstr{I_G1L, (uint8_t)b, 0, 0, (uint16_t)coef_at[i], 0};
+      else P.prog[nprog++] = TInstr{I_G1R, (uint8_t)reg_of(b), 0, 0, (uint16_t)coef_at[i], 0};
+    } else {
+      P.prog[nprog++] = TInstr{I_G2R, (uint8_t)reg_of(op.gb[0]), (uint8_t)reg_of(op.gb[1]), 0,
+                               (uint16_t)coef_at[i], 0};
+    }
+  }
+  P.nprog = nprog;
+  const size_t smem = (size_t)P.necoef * sizeof(Coef);
+  static std::atomic<bool> attr[64];
+  int rc = set_smem_attr(k_warp<LAY, RB>, attr);
+  if (rc) return rc;
+  const int64_t nsub = int64_t(1) << (n - 5 - RB);
+  int64_t grid = (nsub + 7) / 8;
+  const int64_t cap = (int64_t)device_sm_count() * 4;
+  if (grid > cap) grid = cap;
+  k_warp<LAY, RB><<<(int)grid, 256, smem, stream>>>(P);
+  return check_cuda(cudaGetLastError());
+}
+
+int warp_rb(int layout) { return layout == C64 ? 4 : 3; }
+
+int launch_warp_block(const void* in, void* out, int n, int layout, const std::vector<HostOp>& ops,
+                      const std::vector<int>& idx, int rb, cudaStream_t stream) {
+#define QF_WARP_CASE(LAYV)                                                    \
+  switch (rb) {                                                               \
+    case 2: return launch_warp_t<LAYV, 2>(in, out, n, ops, idx, stream);      \
+    case 3: return launch_warp_t<LAYV, 3>(in, out, n, ops, idx, stream);      \
+    case 4: return launch_warp_t<LAYV, 4>(in, out, n, ops, idx, stream);      \
+  }                                                                           \
+  return QF_ERR_NOT_SUPPORTED;
+  switch (layout) {
+    case C64: { QF_WARP_CASE(C64) }
+    case C128: { QF_WARP_CASE(C128) }
+    case FF: { QF_WARP_CASE(FF) }
+  }
+#undef QF_WARP_CASE
+  return QF_ERR_LAYOUT;
 }
 
 int launch_tile_block(const void* in, void* out, int n, int layout, const std::vector<HostOp>& ops,
@@ -873,10 +1484,12 @@ int launch_tile_block(const void* in, void* out, int n, int layout, const std::v
 // Greedy fusion: walk the ops in order; element-wise ops join the current
 // block unconditionally (they need no tile bits), every other op joins while
 // the union of high bits (>= Lmin) stays within fusion_k.
+int g_default_fusion[3] = {4, 3, 3};  // per layout (C64, C128, FF): warp-tile capacity
+
 int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
             cudaStream_t stream, int* passes_out) {
-  const int Lmin = layout == C64 ? 6 : 5;
-  if (fusion_k <= 0) fusion_k = 6;
+  const int Lmin = 5;  // bits 0..4 are the lane bits of every fused kernel
+  if (fusion_k <= 0) fusion_k = g_default_fusion[layout];
   if (fusion_k > 8) fusion_k = 8;
   int passes = 0;
   const void* src = in;
@@ -932,8 +1545,17 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
                         stream);
       rc = launch_single(src, out, n, layout, first, stream);
     } else {
-      LaunchTimer timer(QF_KERNEL_FUSED_TILE, stream);
-      rc = launch_tile_block(src, out, n, layout, ops, b.idx, b.hmask, stream);
+      int hb = __builtin_popcountll(b.hmask & ~((uint64_t(1) << Lmin) - 1));
+      int rb = g_warp_rb_override > 0 ? g_warp_rb_override : warp_rb(layout);
+      rc = QF_ERR_NOT_SUPPORTED;
+      if (!g_force_smem_tile && hb <= rb) {
+        LaunchTimer timer(QF_KERNEL_WARP_TILE, stream);
+        rc = launch_warp_block(src, out, n, layout, ops, b.idx, rb, stream);
+      }
+      if (rc == QF_ERR_NOT_SUPPORTED) {
+        LaunchTimer timer(QF_KERNEL_FUSED_TILE, stream);
+        rc = launch_tile_block(src, out, n, layout, ops, b.idx, b.hmask, stream);
+      }
     }
     if (rc) return rc;
     ++passes;

@@ -38,6 +38,59 @@ struct TileOp {
   uint16_t ncoef;   // number of coefficients (OP_CUT: table size, index clamp)
 };
 
+// Register-resident tile program (k_tile2).  Each of the 256 threads owns
+// 2^RB amplitudes of the 2^(RB+8)-amplitude tile: local bits 0..4 are the
+// lane index, RB local bits index the thread's registers and 3 index the
+// warp, as given by the current TMap.  Gates on register bits run in
+// registers, gates on lane bits through warp shuffles; a MAP instruction
+// re-distributes the tile through shared memory.
+enum TInstrCode : uint8_t {
+  I_MAP = 1,   // a: map index; (re)load registers under that bit map
+  I_G1R = 2,   // a: register bit; coef: 4 coefficients
+  I_G1L = 3,   // a: lane bit; coef: 4 coefficients
+  I_G2R = 4,   // a: register bit of the matrix MSB, b: of the LSB; 16 coefs
+  I_SEG = 5,   // a: first SegOp, b: count (element-wise ops in registers)
+  I_SMEM = 6,  // a: index into ops[] -- applied in shared memory
+};
+struct TInstr {
+  uint8_t code, a, b, c;
+  uint16_t coef;
+  uint16_t pad;
+};
+struct TMap {
+  uint8_t rpos[4];  // local bit of register-index bit j
+  uint8_t wpos[3];  // local bit of warp-index bit i
+  uint8_t pad0;
+  uint8_t rglob[4];  // global bit positions of the same bits
+  uint8_t wglob[3];
+  uint8_t pad1;
+};
+struct SegOp {
+  uint8_t type, k;
+  uint8_t gb[3];
+  uint8_t pad[3];
+  uint16_t coef, ncoef;  // into the element-wise coefficient table
+  uint32_t pad2;
+  uint64_t mask;  // OP_SIGN: the k global bits
+};
+// Warp-tile programs (k_warp): a sub-tile is 32 lanes (global bits 0..4)
+// x 2^RB registers (the block's RB high bits hb[]), streamed straight from
+// global memory; warps never synchronise with each other.
+struct WarpParams {
+  const void* in;
+  void* out;
+  const uint16_t* cuts;
+  int32_t n, rb, nprog, necoef;
+  uint8_t hb[4];  // global bits indexing the registers, ascending
+  TInstr prog[160];
+  SegOp segs[64];
+  Coef coef[1152];
+};
+
+constexpr int TILE_MAX_PROG = 160;
+constexpr int TILE_MAX_MAPS = 48;
+constexpr int TILE_MAX_SEGS = 64;
+
 struct TileParams {
   const void* in;
   void* out;
@@ -47,8 +100,13 @@ struct TileParams {
   int32_t nh;            // extra high tile bits
   int32_t nops;
   int32_t threads;
+  int32_t nprog;         // k_tile2 program length (0: use k_tile)
+  int32_t necoef;        // element-wise coefficients at coef[0, necoef)
   uint8_t hb[8];         // high tile bits (global positions), ascending
   TileOp ops[TILE_MAX_OPS];
+  TInstr prog[TILE_MAX_PROG];
+  TMap maps[TILE_MAX_MAPS];
+  SegOp segs[TILE_MAX_SEGS];
   Coef coef[TILE_MAX_COEF];
 };
 

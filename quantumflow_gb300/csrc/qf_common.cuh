@@ -112,8 +112,52 @@ QF_D double2 cdot(const Coef* u, const double2* a) {
   return make_double2(re, im);
 }
 
+// Error-free product terms: p = ah*bh rounded, c = its rounding error plus
+// the ah*bl and al*bh cross terms (the al*bl term, 2^-48 relative, is
+// dropped).
+QF_D void ff_term(float ah, float al, float bh, float bl, float& p, float& c) {
+  p = __fmul_rn(ah, bh);
+  c = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, __fmaf_rn(ah, bh, -p)));
+}
+// Float-float sum of four product terms, summed as a TwoSum tree (depth 2)
+// with all rounding errors gathered into the low word.
+QF_D void ff_sum4(const float (&p)[4], const float (&c)[4], float& hi, float& lo) {
+  float s01, t01, s23, t23, s, t;
+  two_sum(p[0], p[1], s01, t01);
+  two_sum(p[2], p[3], s23, t23);
+  two_sum(s01, s23, s, t);
+  const float e = __fadd_rn(__fadd_rn(__fadd_rn(c[0], c[1]), __fadd_rn(c[2], c[3])),
+                            __fadd_rn(__fadd_rn(t01, t23), t));
+  fast_two_sum(s, e, hi, lo);
+}
+// (u0 a0 + u1 a1) for float-float complex values, all parts dense.
+QF_D float4 ff_cmac2(float4 u0, float4 a0, float4 u1, float4 a1) {
+  float p[4], c[4];
+  float4 r;
+  ff_term(u0.x, u0.y, a0.x, a0.y, p[0], c[0]);
+  ff_term(-u0.z, -u0.w, a0.z, a0.w, p[1], c[1]);
+  ff_term(u1.x, u1.y, a1.x, a1.y, p[2], c[2]);
+  ff_term(-u1.z, -u1.w, a1.z, a1.w, p[3], c[3]);
+  ff_sum4(p, c, r.x, r.y);
+  ff_term(u0.x, u0.y, a0.z, a0.w, p[0], c[0]);
+  ff_term(u0.z, u0.w, a0.x, a0.y, p[1], c[1]);
+  ff_term(u1.x, u1.y, a1.z, a1.w, p[2], c[2]);
+  ff_term(u1.z, u1.w, a1.x, a1.y, p[3], c[3]);
+  ff_sum4(p, c, r.z, r.w);
+  return r;
+}
+
 template <int J>
 QF_D float4 cdot(const Coef* u, const float4* a) {
+  if constexpr (J == 2) {
+    // dense 2x2 rows (Haar-random gates): the tree form; rows with zero
+    // parts (RX, RY, H ...) take the skipping loop below
+    if (u[0].f[0] != 0.f && u[0].f[2] != 0.f && u[1].f[0] != 0.f && u[1].f[2] != 0.f) {
+      const float4 u0 = make_float4(u[0].f[0], u[0].f[1], u[0].f[2], u[0].f[3]);
+      const float4 u1 = make_float4(u[1].f[0], u[1].f[1], u[1].f[2], u[1].f[3]);
+      return ff_cmac2(u0, a[0], u1, a[1]);
+    }
+  }
   FFAcc re, im;
   re.zero();
   im.zero();
@@ -158,23 +202,7 @@ QF_D double2 cmul_add2(double2 u0, double2 a0, double2 u1, double2 a1) {
   im = fma(u1.y, a1.x, im);
   return make_double2(re, im);
 }
-QF_D float4 cmul_add2(float4 u0, float4 a0, float4 u1, float4 a1) {
-  FFAcc re, im;
-  re.zero();
-  im.zero();
-  re.add_prod(u0.x, u0.y, a0.x, a0.y);
-  re.add_prod(-u0.z, -u0.w, a0.z, a0.w);
-  re.add_prod(u1.x, u1.y, a1.x, a1.y);
-  re.add_prod(-u1.z, -u1.w, a1.z, a1.w);
-  im.add_prod(u0.x, u0.y, a0.z, a0.w);
-  im.add_prod(u0.z, u0.w, a0.x, a0.y);
-  im.add_prod(u1.x, u1.y, a1.z, a1.w);
-  im.add_prod(u1.z, u1.w, a1.x, a1.y);
-  float4 r;
-  re.finish(r.x, r.y);
-  im.finish(r.z, r.w);
-  return r;
-}
+QF_D float4 cmul_add2(float4 u0, float4 a0, float4 u1, float4 a1) { return ff_cmac2(u0, a0, u1, a1); }
 
 // single complex multiply by a uniform coefficient
 QF_D float2 cmul(const Coef& u, float2 a) { return cdot<1>(&u, &a); }
@@ -264,6 +292,7 @@ QF_D void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
 }
 QF_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 QF_D void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+QF_D void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 QF_D void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 QF_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

@@ -19,9 +19,17 @@ def _circuit_from_fixture(c, N):
     return circ
 
 
+@pytest.fixture(params=[0, 1, 2, 4], ids=["default", "smem_tiles", "warp_rb2", "warp_rb4"])
+def tile_kernel(request):
+    from quantumflow_gb300 import _native as nat
+    nat.call("qf_set_tile_kernel", request.param)
+    yield request.param
+    nat.call("qf_set_tile_kernel", 0)
+
+
 @pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-5)])
 @pytest.mark.parametrize("fusion_k", [1, 2, 4, 6, 8])
-def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k):
+def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k, tile_kernel):
     import quantumflow_gb300 as qf
     c = golden["circuits"]
     for N in (4, 6, 9, 12):
@@ -74,8 +82,11 @@ def test_gops_circuit(golden):
     assert np.max(np.abs(ket.asarray().reshape(-1) - c["gops_state"])) < 1e-12
 
 
-@pytest.mark.parametrize("N", [16, 22])
-def test_fused_equals_unfused_and_oracle(N):
+@pytest.mark.parametrize("N", [13, 16, 22])
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_fused_equals_unfused_and_oracle(N, dtype, tile_kernel):
+    """Mixed gate classes through every fused-kernel instruction: 1q gates on
+    lane, register and warp bits, 2q dense gates, permutations, diagonals."""
     import quantumflow_gb300 as qf
     rng = np.random.default_rng(N)
     circ = qf.Circuit()
@@ -85,15 +96,23 @@ def test_fused_equals_unfused_and_oracle(N):
         perm = rng.permutation(N)
         for a in range(0, N - 1, 2):
             circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
-    fused = circ.run(qf.zero_state(N), fusion_k=6)
-    unfused = circ.run(qf.zero_state(N), fusion_k=1)
+        circ += qf.random_gate([N - 6, N - 8], random_state=rng)
+        circ += qf.random_gate([1, N - 1], random_state=rng)
+        circ += qf.random_gate([3, 2], random_state=rng)
+        circ += qf.CNOT(N - 7, 2)
+        circ += qf.ZZ(0.3, 0, N - 2)
+        circ += qf.CCNOT(5, 0, N - 3)
+        circ += qf.random_gate([6, 7, 8], random_state=rng)
+    tol = 1e-12 if dtype == "complex128" else 2e-5
+    fused = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=6)
+    unfused = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=1)
     assert circ.last_passes == len(circ.elements)
     a, b = fused.asarray(), unfused.asarray()
-    assert np.max(np.abs(a - b)) < 1e-12
+    assert np.max(np.abs(a - b)) < tol
     if N <= 16:
         ops = [(g.asoperator(), tuple(g.qubits)) for g in circ]
         ref = orc.run_ops(orc.zero_state(N), ops)
-        assert np.max(np.abs(a - ref)) < 1e-12
+        assert np.max(np.abs(a - ref)) < tol
 
 
 @pytest.mark.parametrize("N", [26])
