@@ -151,6 +151,32 @@ int qf_qaoa_expectation_grad(void* psi, int n, int layout, const uint16_t* cuts,
                              int fusion_k, double* out, void* workspace, size_t workspace_bytes,
                              void* stream);
 
+/* ------------------------------------------------- batched QAOA ---------- */
+/* Many independent QAOA MAXCUT instances (uneven n, graphs, depths) in one
+ * persistent launch: forward <C> and its adjoint gradient per instance.  No
+ * reference counterpart (the reference evaluates one circuit at a time,
+ * quantumflow/qaoa.py:22-81, examples/qaoa_maxcut.py:37-87).  All pointers
+ * are device pointers; the launch is asynchronous and contains only device
+ * work (a counter reset and one kernel), so it can be captured in a CUDA
+ * graph and replayed after the angles are updated in place. */
+typedef struct qf_batch_instance {
+  int32_t n;            /* qubits, 1..max_n (and <= 2*tile_bits)              */
+  int32_t p;            /* QAOA layers, 0..64                                 */
+  int32_t nedges;       /* unweighted edges, 0..1023                          */
+  int32_t edge_offset;  /* first edge: axis pairs at edges[2*edge_offset]     */
+  int32_t angle_offset; /* beta[p] then gamma[p] at angles[angle_offset]      */
+  int32_t out_offset;   /* d/dgamma[p], d/dbeta[p], <C> at out[out_offset]    */
+} qf_batch_instance;
+/* Workspace for `ctas` persistent CTAs and instances of up to max_n qubits. */
+size_t qf_batch_workspace_bytes(int max_n, int layout, int ctas);
+/* layout QF_LAYOUT_C64 or QF_LAYOUT_FF; tile_bits 8..12 (C64) / 8..11 (FF):
+ * instances with n <= tile_bits stay in shared memory.  Order instances
+ * largest first for load balance.  A malformed instance gets NaN outputs and
+ * raises bit 1 of the device error word. */
+int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, const uint8_t* edges,
+                       const double* angles, double* out, int layout, int max_n, int tile_bits, int ctas,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------- reductions ------- */
 /* All reductions write their result to DEVICE memory `out` and need a
  * workspace of qf_reduce_workspace_bytes(n) bytes (device, 256-byte aligned).

@@ -76,6 +76,8 @@ SIGNATURES = {
     "qf_qaoa_state": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int, _vp]),
     "qf_expectation_cuts": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
     "qf_qaoa_grad_workspace_bytes": (_sz, [_c_int, _c_int, _c_int]),
+    "qf_batch_workspace_bytes": (_sz, [_c_int, _c_int, _c_int]),
+    "qf_batch_qaoa_grad": (_c_int, [_vp, _c_int, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _sz, _vp]),
     "qf_qaoa_expectation_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int,
                                           _vp, _vp, _sz, _vp]),
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),

@@ -1,0 +1,189 @@
+"""Batched QAOA MAXCUT: thousands of uneven instances per launch.
+
+``QAOABatch`` uploads the instances once (graphs as axis pairs, depths,
+angle and output offsets), orders them largest first, and evaluates every
+instance's <C> and adjoint gradient with one persistent kernel
+(``qf_batch_qaoa_grad``).  The launch (a counter reset plus the kernel) and
+an optional on-device Adam update are captured in a CUDA graph and replayed.
+
+The reference evaluates one circuit at a time (quantumflow/qaoa.py:22-81,
+examples/qaoa_maxcut.py:37-87); each instance here computes exactly that
+circuit's expectation and its gradient.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .qaoa import _graph_arrays
+
+__all__ = ["QAOABatch"]
+
+
+class _Instance(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("p", ctypes.c_int32), ("nedges", ctypes.c_int32),
+                ("edge_offset", ctypes.c_int32), ("angle_offset", ctypes.c_int32),
+                ("out_offset", ctypes.c_int32)]
+
+
+_LAYOUTS = {"complex64": nat.LAYOUT_C64, "complex128": nat.LAYOUT_FF}
+
+
+class QAOABatch:
+    """Forward expectation + adjoint gradient of many QAOA MAXCUT instances.
+
+    Args:
+        graphs: unweighted graphs (networkx or :class:`qaoa.Graph`).
+        ps: QAOA depth per graph (int or sequence).
+        dtype: 'complex64' (FP32) or 'complex128' (float-float arithmetic).
+        tile_bits, ctas: kernel shape; None takes the autotuned or default
+            values (see :mod:`quantumflow_gb300.autotune`).
+    """
+
+    def __init__(self, graphs, ps, dtype="complex64", tile_bits=None, ctas=None, device=None):
+        if dtype not in _LAYOUTS:
+            raise ValueError("dtype must be complex64 or complex128")
+        self.dtype = dtype
+        self.layout = _LAYOUTS[dtype]
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        graphs = list(graphs)
+        ps = [int(ps)] * len(graphs) if np.isscalar(ps) else [int(p) for p in ps]
+        if len(ps) != len(graphs):
+            raise ValueError("one depth per graph")
+        self.count = len(graphs)
+        self.ns = np.zeros(self.count, dtype=np.int64)
+        self.ps = np.asarray(ps, dtype=np.int64)
+        self.nedges = np.zeros(self.count, dtype=np.int64)
+        edges_all = []
+        for i, g in enumerate(graphs):
+            nodes, edges, weights, node_w = _graph_arrays(g)
+            if any(w != 1.0 for w in weights) or any(w is not None for w in node_w):
+                raise ValueError("the batched kernel handles unweighted graphs without node weights")
+            self.ns[i] = len(nodes)
+            self.nedges[i] = len(edges)
+            edges_all.append(np.asarray(edges, dtype=np.uint8).reshape(-1, 2))
+        self.max_n = int(self.ns.max()) if self.count else 1
+        ts_max = 12 if self.layout == nat.LAYOUT_C64 else 11
+        if self.max_n > 2 * ts_max:
+            raise ValueError(f"instances above {2 * ts_max} qubits are not supported by the batch kernel")
+        # offsets in the caller's (input) order; launch order is largest first
+        self.angle_offset = np.concatenate([[0], np.cumsum(2 * self.ps)[:-1]]).astype(np.int64)
+        self.out_offset = np.concatenate([[0], np.cumsum(2 * self.ps + 1)[:-1]]).astype(np.int64)
+        edge_offset = np.concatenate([[0], np.cumsum(self.nedges)[:-1]]).astype(np.int64)
+        order = sorted(range(self.count), key=lambda i: (-(2 ** self.ns[i]) * (self.ps[i] + 1), i))
+        inst = (_Instance * max(1, self.count))()
+        for k, i in enumerate(order):
+            inst[k] = _Instance(int(self.ns[i]), int(self.ps[i]), int(self.nedges[i]), int(edge_offset[i]),
+                                int(self.angle_offset[i]), int(self.out_offset[i]))
+        raw = np.frombuffer(bytes(inst), dtype=np.uint8)
+        self.d_inst = torch.from_numpy(raw.copy()).to(self.device)
+        edges = np.concatenate(edges_all) if edges_all else np.zeros((0, 2), np.uint8)
+        self.d_edges = torch.from_numpy(np.ascontiguousarray(edges).reshape(-1)).to(self.device)
+        if self.d_edges.numel() == 0:
+            self.d_edges = torch.zeros(2, dtype=torch.uint8, device=self.device)
+        self.angles = torch.zeros(int(2 * self.ps.sum()), dtype=torch.float64, device=self.device)
+        self.out = torch.zeros(int((2 * self.ps + 1).sum()), dtype=torch.float64, device=self.device)
+        # index maps: angles (beta..., gamma...) <- out (dgamma..., dbeta..., E)
+        gsrc = np.zeros(self.angles.numel(), dtype=np.int64)
+        esrc = np.zeros(self.count, dtype=np.int64)
+        for i in range(self.count):
+            p, a, o = int(self.ps[i]), int(self.angle_offset[i]), int(self.out_offset[i])
+            gsrc[a:a + p] = o + p + np.arange(p)      # beta  <- dbeta
+            gsrc[a + p:a + 2 * p] = o + np.arange(p)  # gamma <- dgamma
+            esrc[i] = o + 2 * p
+        self._gsrc = torch.from_numpy(gsrc).to(self.device)
+        self._esrc = torch.from_numpy(esrc).to(self.device)
+        from . import autotune
+        cfg = autotune.batch_config(self) if (tile_bits is None or ctas is None) else {}
+        self.tile_bits = int(tile_bits if tile_bits is not None else cfg.get("tile_bits", ts_max))
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+        self.ctas = int(ctas if ctas is not None else cfg.get("ctas", 2 * sms))
+        self._alloc_workspace()
+        self._graph = None
+
+    def _alloc_workspace(self):
+        self.ws_bytes = nat.lib.qf_batch_workspace_bytes(self.max_n, self.layout, self.ctas)
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+
+    # ------------------------------------------------------------ angles ---
+    def set_angles(self, betas, gammas):
+        """Per-instance beta and gamma sequences (lists of length-p arrays)."""
+        host = np.zeros(self.angles.numel())
+        for i in range(self.count):
+            p, a = int(self.ps[i]), int(self.angle_offset[i])
+            host[a:a + p] = np.asarray(betas[i], dtype=np.float64).reshape(p)
+            host[a + p:a + 2 * p] = np.asarray(gammas[i], dtype=np.float64).reshape(p)
+        self.angles.copy_(torch.from_numpy(host))
+
+    def get_angles(self):
+        host = self.angles.cpu().numpy()
+        betas, gammas = [], []
+        for i in range(self.count):
+            p, a = int(self.ps[i]), int(self.angle_offset[i])
+            betas.append(host[a:a + p].copy())
+            gammas.append(host[a + p:a + 2 * p].copy())
+        return betas, gammas
+
+    # ------------------------------------------------------------ launch ---
+    def launch(self, stream=None):
+        """Enqueue one evaluation (asynchronous)."""
+        nat.call("qf_batch_qaoa_grad", nat.ptr(self.d_inst), self.count, nat.ptr(self.d_edges),
+                 nat.ptr(self.angles), nat.ptr(self.out), self.layout, self.max_n, self.tile_bits,
+                 self.ctas, nat.ptr(self.ws), self.ws_bytes, stream or nat.stream_handle(self.device))
+
+    def expectations(self) -> torch.Tensor:
+        """<C> per instance (device tensor, input order) from the last launch."""
+        return self.out[self._esrc]
+
+    def angle_gradients(self) -> torch.Tensor:
+        """d<C>/d angles in the layout of ``self.angles`` (device)."""
+        return self.out[self._gsrc]
+
+    def evaluate(self):
+        """Run once; return (E, dbetas, dgammas) on the host (input order)."""
+        self.launch()
+        o = self.out.cpu().numpy()
+        es, dbs, dgs = [], [], []
+        for i in range(self.count):
+            p, off = int(self.ps[i]), int(self.out_offset[i])
+            dgs.append(o[off:off + p].copy())
+            dbs.append(o[off + p:off + 2 * p].copy())
+            es.append(o[off + 2 * p])
+        return np.array(es), dbs, dgs
+
+    # ------------------------------------------------------------ Adam -----
+    def adam(self, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8, use_graph=True):
+        """Gradient ascent on every instance's <C> with Adam, all on the
+        device; one CUDA-graph replay per step (launch + update)."""
+        m = torch.zeros_like(self.angles)
+        v = torch.zeros_like(self.angles)
+        b1, b2 = betas
+        t = torch.zeros(1, dtype=torch.float64, device=self.device)
+
+        def step():
+            self.launch(nat.stream_handle(self.device))
+            g = self.out[self._gsrc]
+            t.add_(1.0)
+            m.mul_(b1).add_(g, alpha=1 - b1)
+            v.mul_(b2).addcmul_(g, g, value=1 - b2)
+            mhat = m / (1 - b1 ** t)
+            vhat = v / (1 - b2 ** t)
+            self.angles.add_(lr * mhat / (vhat.sqrt() + eps))
+
+        if not use_graph or steps < 3:
+            for _ in range(steps):
+                step()
+            return
+        step()  # warm-up outside capture (sets kernel attributes, caches)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                step()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        for _ in range(steps - 1):  # capture records without running
+            g.replay()
+        self._graph = g

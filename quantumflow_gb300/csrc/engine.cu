@@ -41,6 +41,19 @@ int read_clear_device_error(int* flags, cudaStream_t stream) {
   return check_cuda(cudaStreamSynchronize(stream));
 }
 
+// Device address of the error word, for kernels in other translation units.
+int* device_error_word() {
+  static int* addr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_qf_device_error) != cudaSuccess) return nullptr;
+    addr[dev] = static_cast<int*>(p);
+  }
+  return addr[dev];
+}
+
 int device_sm_count() {
   static std::atomic<int> cache[64];
   int dev = 0;

@@ -1,0 +1,128 @@
+"""Batched QAOA (one persistent launch for many uneven instances) against the
+single-instance adjoint path, the CPU oracle, and reference fixtures."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import qf_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_instances(count, seed, nmin=4, nmax=13, pmax=4):
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(seed)
+    graphs, ps = [], []
+    for i in range(count):
+        n = int(rng.integers(nmin, nmax + 1))
+        if i % 2 and n % 2 == 0 and n > 3:
+            g = qf.qaoa.random_regular_graph(3, n, seed=int(rng.integers(1 << 30)))
+        else:
+            g = qf.qaoa.gnp_random_graph(n, 0.5, seed=int(rng.integers(1 << 30)))
+        graphs.append(g)
+        ps.append(int(rng.integers(1, pmax + 1)))
+    return graphs, ps, rng
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex64", 2e-4), ("complex128", 1e-9)])
+def test_batch_matches_single_instance(dtype, tol):
+    import quantumflow_gb300 as qf
+    graphs, ps, rng = _mixed_instances(40, 5)
+    betas = [rng.uniform(0, np.pi, p) for p in ps]
+    gammas = [rng.uniform(0, np.pi, p) for p in ps]
+    batch = qf.batched.QAOABatch(graphs, ps, dtype=dtype)
+    batch.set_angles(betas, gammas)
+    es, dbs, dgs = batch.evaluate()
+    for i in range(len(graphs)):
+        prob = qf.QAOAMaxCut(graphs[i], ps[i])
+        e, gb, gg = prob.expectation_and_grad(betas[i], gammas[i])
+        scale = max(1.0, abs(e))
+        assert abs(es[i] - e) < tol * scale, (i, es[i], e)
+        np.testing.assert_allclose(dbs[i], gb, atol=tol * scale * 4)
+        np.testing.assert_allclose(dgs[i], gg, atol=tol * scale * 4)
+    from quantumflow_gb300 import _native as nat
+    assert nat.device_error() == 0
+
+
+@pytest.mark.parametrize("tile_bits", [8, 10])
+def test_batch_large_instances_tiled(tile_bits):
+    """Instances above the tile size run the global-scratch tiled passes."""
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(9)
+    graphs = [qf.qaoa.random_regular_graph(3, n, seed=n) for n in (12, 14, 16, 10)]
+    ps = [3, 2, 2, 4]
+    betas = [rng.uniform(0, np.pi, p) for p in ps]
+    gammas = [rng.uniform(0, np.pi, p) for p in ps]
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128", tile_bits=tile_bits, ctas=8)
+    batch.set_angles(betas, gammas)
+    es, dbs, dgs = batch.evaluate()
+    for i, g in enumerate(graphs):
+        e, gb, gg = qf.QAOAMaxCut(g, ps[i]).expectation_and_grad(betas[i], gammas[i])
+        assert abs(es[i] - e) < 1e-9
+        np.testing.assert_allclose(dbs[i], gb, atol=1e-8)
+        np.testing.assert_allclose(dgs[i], gg, atol=1e-8)
+
+
+def test_batch_reference_fixtures(golden):
+    import quantumflow_gb300 as qf
+    q = golden["qaoa"]
+    names = ["c1", "reg8", "reg10", "er9"]
+    graphs = []
+    for name in names:
+        g = qf.Graph(nodes=range(int(q[f"{name}_n"])))
+        for a, b in q[f"{name}_edges"]:
+            g.add_edge(int(a), int(b))
+        graphs.append(g)
+    ps = [int(q[f"{name}_p"]) for name in names]
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128")
+    batch.set_angles([q[f"{n}_beta"] for n in names], [q[f"{n}_gamma"] for n in names])
+    es, dbs, dgs = batch.evaluate()
+    for i, name in enumerate(names):
+        assert abs(es[i] - float(q[f"{name}_expectation"])) < 1e-10
+        np.testing.assert_allclose(dbs[i], q[f"{name}_fd_grad_beta"], atol=2e-7)
+        np.testing.assert_allclose(dgs[i], q[f"{name}_fd_grad_gamma"], atol=2e-7)
+
+
+def test_batch_adam_graph_replay_improves_all():
+    import quantumflow_gb300 as qf
+    graphs, ps, rng = _mixed_instances(64, 3, nmin=6, nmax=12, pmax=3)
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex64")
+    betas = [np.full(p, 0.3) for p in ps]
+    gammas = [np.full(p, 0.3) for p in ps]
+    batch.set_angles(betas, gammas)
+    e0, _, _ = batch.evaluate()
+    batch.adam(30, lr=0.05, use_graph=True)
+    e1, _, _ = batch.evaluate()
+    assert np.all(e1 >= e0 - 1e-4)
+    assert np.mean(e1 - e0) > 0.05
+    # the graph replays equal eager steps
+    batch.set_angles(betas, gammas)
+    batch.adam(30, lr=0.05, use_graph=False)
+    e2, _, _ = batch.evaluate()
+    np.testing.assert_allclose(e2, e1, rtol=1e-5, atol=1e-5)
+
+
+def test_batch_malformed_instance_is_skipped():
+    import ctypes
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    g = qf.qaoa.gnp_random_graph(6, 0.5, seed=1)
+    batch = qf.batched.QAOABatch([g, g], [2, 2], dtype="complex64")
+    raw = batch.d_inst.cpu().numpy().view(np.int32).reshape(-1, 6).copy()
+    raw[0, 0] = 40  # n above max_n
+    batch.d_inst.copy_(torch.from_numpy(raw.view(np.uint8).reshape(-1)))
+    batch.set_angles([np.ones(2)] * 2, [np.ones(2)] * 2)
+    es, _, _ = batch.evaluate()
+    assert np.isnan(es).sum() == 1
+    assert nat.device_error() == 2
+
+
+def test_autotune_batch(tmp_path, monkeypatch):
+    import quantumflow_gb300 as qf
+    monkeypatch.setenv("QUANTUMFLOW_GB300_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    graphs, ps, rng = _mixed_instances(32, 7, nmin=8, nmax=14)
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex64", tile_bits=12, ctas=152)
+    best = qf.autotune.tune_batch(batch, ctas_per_sm=(1, 2), reps=1)
+    assert best["tile_bits"] >= 8 and best["ctas"] > 0 and len(best["trials"]) >= 2
+    again = qf.batched.QAOABatch(graphs, ps, dtype="complex64")
+    assert (again.tile_bits, again.ctas) == (best["tile_bits"], best["ctas"])
