@@ -177,6 +177,31 @@ int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, const
                        const double* angles, double* out, int layout, int max_n, int tile_bits, int ctas,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------ learned angle initialiser ----- */
+/* A 3-layer message-passing graph network (hidden width 64, FP32) mapping a
+ * graph to 2p QAOA angles (beta_0..beta_{p-1}, gamma_0..gamma_{p-1}); no
+ * reference counterpart (the reference draws initial angles at random,
+ * examples/qaoa_maxcut.py:47-51).  Graph batches are CSR on the device:
+ * graph g owns nodes [node_offset[g], node_offset[g+1]) (1..32 nodes), node
+ * i's neighbours are adj[adj_offset[i] .. adj_offset[i+1]) (global node ids,
+ * both directions listed).  params holds qf_gnn_param_count(p) floats. */
+#define QF_GNN_HIDDEN 64
+#define QF_GNN_MAX_NODES 32
+size_t qf_gnn_param_count(int p);
+/* Activation buffer size (floats) for the backward pass. */
+size_t qf_gnn_activation_floats(int total_nodes, int ngraphs);
+/* out[g][2p] = network(graph g); activations may be NULL (inference). */
+int qf_gnn_forward(const float* params, int p, int ngraphs, int total_nodes, const int32_t* node_offset,
+                   const int32_t* adj_offset, const int32_t* adj, float* out, float* activations, void* stream);
+/* grad += d/dparams of mean((out - target)^2) over the batch (grad must be
+ * zeroed by the caller before the first batch); loss += sum (out-target)^2. */
+int qf_gnn_backward(const float* params, int p, int ngraphs, int total_nodes, const int32_t* node_offset,
+                    const int32_t* adj_offset, const int32_t* adj, const float* out, const float* target,
+                    const float* activations, float* grad, float* loss, void* stream);
+/* One Adam step (Kingma & Ba 2015) on count floats; step counts from 1. */
+int qf_adam_update(float* params, const float* grad, float* m, float* v, int count, float lr, float beta1,
+                   float beta2, float eps, int step, void* stream);
+
 /* ------------------------------------------------------- reductions ------- */
 /* All reductions write their result to DEVICE memory `out` and need a
  * workspace of qf_reduce_workspace_bytes(n) bytes (device, 256-byte aligned).

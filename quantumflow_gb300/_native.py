@@ -77,6 +77,12 @@ SIGNATURES = {
     "qf_expectation_cuts": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
     "qf_qaoa_grad_workspace_bytes": (_sz, [_c_int, _c_int, _c_int]),
     "qf_batch_workspace_bytes": (_sz, [_c_int, _c_int, _c_int]),
+    "qf_gnn_param_count": (_sz, [_c_int]),
+    "qf_gnn_activation_floats": (_sz, [_c_int, _c_int]),
+    "qf_gnn_forward": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qf_gnn_backward": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "qf_adam_update": (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                ctypes.c_float, _c_int, _vp]),
     "qf_batch_qaoa_grad": (_c_int, [_vp, _c_int, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _sz, _vp]),
     "qf_qaoa_expectation_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int,
                                           _vp, _vp, _sz, _vp]),
