@@ -170,10 +170,13 @@ typedef struct qf_batch_instance {
 /* Workspace for `ctas` persistent CTAs and instances of up to max_n qubits. */
 size_t qf_batch_workspace_bytes(int max_n, int layout, int ctas);
 /* layout QF_LAYOUT_C64 or QF_LAYOUT_FF; tile_bits 8..12 (C64) / 8..11 (FF):
- * instances with n <= tile_bits stay in shared memory.  Order instances
- * largest first for load balance.  A malformed instance gets NaN outputs and
- * raises bit 1 of the device error word. */
-int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, const uint8_t* edges,
+ * instances with n <= tile_bits stay in shared memory.  The first nlarge
+ * instances are each processed by a cluster of 8 CTAs (hardware cluster
+ * barriers between passes); the rest by one CTA each.  ctas must be a
+ * multiple of 8.  Order instances largest first within each group.  A
+ * malformed instance gets NaN outputs and raises bit 1 of the device error
+ * word. */
+int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, int nlarge, const uint8_t* edges,
                        const double* angles, double* out, int layout, int max_n, int tile_bits, int ctas,
                        void* workspace, size_t workspace_bytes, void* stream);
 

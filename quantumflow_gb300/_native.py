@@ -83,7 +83,8 @@ SIGNATURES = {
     "qf_gnn_backward": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "qf_adam_update": (_c_int, [_vp, _vp, _vp, _vp, _c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                 ctypes.c_float, _c_int, _vp]),
-    "qf_batch_qaoa_grad": (_c_int, [_vp, _c_int, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _sz, _vp]),
+    "qf_batch_qaoa_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _sz,
+                                    _vp]),
     "qf_qaoa_expectation_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int,
                                           _vp, _vp, _sz, _vp]),
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),

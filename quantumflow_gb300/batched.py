@@ -70,14 +70,7 @@ class QAOABatch:
         # offsets in the caller's (input) order; launch order is largest first
         self.angle_offset = np.concatenate([[0], np.cumsum(2 * self.ps)[:-1]]).astype(np.int64)
         self.out_offset = np.concatenate([[0], np.cumsum(2 * self.ps + 1)[:-1]]).astype(np.int64)
-        edge_offset = np.concatenate([[0], np.cumsum(self.nedges)[:-1]]).astype(np.int64)
-        order = sorted(range(self.count), key=lambda i: (-(2 ** self.ns[i]) * (self.ps[i] + 1), i))
-        inst = (_Instance * max(1, self.count))()
-        for k, i in enumerate(order):
-            inst[k] = _Instance(int(self.ns[i]), int(self.ps[i]), int(self.nedges[i]), int(edge_offset[i]),
-                                int(self.angle_offset[i]), int(self.out_offset[i]))
-        raw = np.frombuffer(bytes(inst), dtype=np.uint8)
-        self.d_inst = torch.from_numpy(raw.copy()).to(self.device)
+        self.edge_offset = np.concatenate([[0], np.cumsum(self.nedges)[:-1]]).astype(np.int64)
         edges = np.concatenate(edges_all) if edges_all else np.zeros((0, 2), np.uint8)
         self.d_edges = torch.from_numpy(np.ascontiguousarray(edges).reshape(-1)).to(self.device)
         if self.d_edges.numel() == 0:
@@ -103,8 +96,25 @@ class QAOABatch:
         self._graph = None
 
     def _alloc_workspace(self):
+        """Upload the launch order for the current tile size and size the
+        workspace.  Instances with n >= tile_bits + 4 go first, each to a
+        cluster of 8 CTAs; the rest follow, one CTA each; both groups are
+        ordered largest first."""
+        self.ctas = max(8, (self.ctas // 8) * 8)
+        coop_min = self.tile_bits + 4
+        cost = lambda i: -(2 ** int(self.ns[i])) * (int(self.ps[i]) + 1)
+        large = sorted((i for i in range(self.count) if self.ns[i] >= coop_min), key=lambda i: (cost(i), i))
+        rest = sorted((i for i in range(self.count) if self.ns[i] < coop_min), key=lambda i: (cost(i), i))
+        self.nlarge = len(large)
+        inst = (_Instance * max(1, self.count))()
+        for k, i in enumerate(large + rest):
+            inst[k] = _Instance(int(self.ns[i]), int(self.ps[i]), int(self.nedges[i]), int(self.edge_offset[i]),
+                                int(self.angle_offset[i]), int(self.out_offset[i]))
+        raw = np.frombuffer(bytes(inst), dtype=np.uint8)
+        self.d_inst = torch.from_numpy(raw.copy()).to(self.device)
         self.ws_bytes = nat.lib.qf_batch_workspace_bytes(self.max_n, self.layout, self.ctas)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+        self._graph = None
 
     # ------------------------------------------------------------ angles ---
     def set_angles(self, betas, gammas):
@@ -128,7 +138,7 @@ class QAOABatch:
     # ------------------------------------------------------------ launch ---
     def launch(self, stream=None):
         """Enqueue one evaluation (asynchronous)."""
-        nat.call("qf_batch_qaoa_grad", nat.ptr(self.d_inst), self.count, nat.ptr(self.d_edges),
+        nat.call("qf_batch_qaoa_grad", nat.ptr(self.d_inst), self.count, self.nlarge, nat.ptr(self.d_edges),
                  nat.ptr(self.angles), nat.ptr(self.out), self.layout, self.max_n, self.tile_bits,
                  self.ctas, nat.ptr(self.ws), self.ws_bytes, stream or nat.stream_handle(self.device))
 
@@ -153,37 +163,81 @@ class QAOABatch:
         return np.array(es), dbs, dgs
 
     # ------------------------------------------------------------ Adam -----
-    def adam(self, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8, use_graph=True):
-        """Gradient ascent on every instance's <C> with Adam, all on the
-        device; one CUDA-graph replay per step (launch + update)."""
-        m = torch.zeros_like(self.angles)
-        v = torch.zeros_like(self.angles)
+    def optimizer_reset(self, maxcut=None, target=None):
+        """Fresh Adam state; optional per-instance max cut and target ratio
+        for recording the first step each instance reaches the target."""
+        self._opt = {
+            "m": torch.zeros_like(self.angles), "v": torch.zeros_like(self.angles),
+            "t": torch.zeros(1, dtype=torch.float64, device=self.device),
+            "first": torch.full((self.count,), -1, dtype=torch.int64, device=self.device),
+            "mc": None if maxcut is None else torch.as_tensor(np.asarray(maxcut, dtype=np.float64),
+                                                              device=self.device),
+            "target": None if target is None else float(target),
+        }
+        self._graph = None
+        self._graph_key = None
+
+    def _opt_step(self, lr, b1, b2, eps):
+        o = self._opt
+        self.launch(nat.stream_handle(self.device))
+        if o["mc"] is not None and o["target"] is not None:
+            hit = (self.out[self._esrc] / o["mc"] >= o["target"]) & (o["first"] < 0)
+            o["first"].copy_(torch.where(hit, o["t"].to(torch.int64).expand_as(o["first"]), o["first"]))
+        g = self.out[self._gsrc]
+        o["t"].add_(1.0)
+        o["m"].mul_(b1).add_(g, alpha=1 - b1)
+        o["v"].mul_(b2).addcmul_(g, g, value=1 - b2)
+        mhat = o["m"] / (1 - b1 ** o["t"])
+        vhat = o["v"] / (1 - b2 ** o["t"])
+        self.angles.add_(lr * mhat / (vhat.sqrt() + eps))
+
+    def optimize(self, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8, maxcut=None, target=None,
+                 use_graph=True, reset=True):
+        """Gradient ascent on every instance's <C> with Adam, entirely on the
+        device: each step is one batched forward + adjoint launch and the
+        update, replayed from a CUDA graph.  ``reset=False`` continues the
+        previous optimizer state (chunked runs).
+
+        With ``maxcut`` (per instance, input order) and ``target`` the step at
+        which each instance first has <C>/maxcut >= target is recorded (-1 if
+        never; the ratio is that of the angles a step starts from).  Returns
+        (ratios or <C> at the final angles, first_step)."""
+        if reset or getattr(self, "_opt", None) is None:
+            self.optimizer_reset(maxcut, target)
         b1, b2 = betas
-        t = torch.zeros(1, dtype=torch.float64, device=self.device)
+        key = (float(lr), b1, b2, eps)
+        if steps > 0:
+            if not use_graph:
+                for _ in range(steps):
+                    self._opt_step(lr, b1, b2, eps)
+            else:
+                done = 0
+                if self._graph is None or self._graph_key != key:
+                    self._opt_step(lr, b1, b2, eps)  # outside capture: sets attributes, caches
+                    done = 1
+                    torch.cuda.synchronize(self.device)
+                    graph = torch.cuda.CUDAGraph()
+                    s = torch.cuda.Stream(self.device)
+                    s.wait_stream(torch.cuda.current_stream(self.device))
+                    with torch.cuda.stream(s):
+                        with torch.cuda.graph(graph, stream=s):
+                            self._opt_step(lr, b1, b2, eps)  # recorded, not run
+                    torch.cuda.current_stream(self.device).wait_stream(s)
+                    self._graph, self._graph_key = graph, key
+                for _ in range(steps - done):
+                    self._graph.replay()
+        o = self._opt
+        self.launch()
+        e = self.out[self._esrc]
+        first = o["first"]
+        if o["mc"] is not None and o["target"] is not None:
+            ratio = e / o["mc"]
+            hit = (ratio >= o["target"]) & (first < 0)
+            first = torch.where(hit, o["t"].to(torch.int64).expand_as(first), first)
+            o["first"].copy_(first)
+            return ratio.cpu().numpy(), first.cpu().numpy()
+        return e.cpu().numpy(), first.cpu().numpy()
 
-        def step():
-            self.launch(nat.stream_handle(self.device))
-            g = self.out[self._gsrc]
-            t.add_(1.0)
-            m.mul_(b1).add_(g, alpha=1 - b1)
-            v.mul_(b2).addcmul_(g, g, value=1 - b2)
-            mhat = m / (1 - b1 ** t)
-            vhat = v / (1 - b2 ** t)
-            self.angles.add_(lr * mhat / (vhat.sqrt() + eps))
-
-        if not use_graph or steps < 3:
-            for _ in range(steps):
-                step()
-            return
-        step()  # warm-up outside capture (sets kernel attributes, caches)
-        torch.cuda.synchronize(self.device)
-        g = torch.cuda.CUDAGraph()
-        s = torch.cuda.Stream(self.device)
-        s.wait_stream(torch.cuda.current_stream(self.device))
-        with torch.cuda.stream(s):
-            with torch.cuda.graph(g, stream=s):
-                step()
-        torch.cuda.current_stream(self.device).wait_stream(s)
-        for _ in range(steps - 1):  # capture records without running
-            g.replay()
-        self._graph = g
+    def adam(self, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8, use_graph=True):
+        """Adam ascent on every instance's <C> (see :meth:`optimize`)."""
+        self.optimize(steps, lr=lr, betas=betas, eps=eps, use_graph=use_graph)

@@ -21,6 +21,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "engine.cuh"
 #include "state.cuh"
 
@@ -33,6 +35,7 @@ static_assert(sizeof(BatchInstanceDev) == sizeof(qf_batch_instance), "layout mis
 
 constexpr int BATCH_MAX_EDGES = 1023;
 constexpr int BATCH_THREADS = 256;
+constexpr int BATCH_CLUSTER = 8;  // CTAs that share one large instance
 
 // ---------------------------------------------------------- arithmetic ----
 template <int LAY>
@@ -211,16 +214,222 @@ __device__ void tile_apply_b(const TileOpsB& T, E* sp, E* sl, const uint16_t* sc
 struct BatchParams {
   const BatchInstanceDev* inst;
   int ninst;
+  int nlarge;            // instances [0, nlarge) are processed by whole clusters
   const uint8_t* edges;  // axis pairs
   const double* angles;  // per instance: beta[p], gamma[p]
   double* out;           // per instance: dgamma[p], dbeta[p], <C>
   char* scratch;         // per CTA: psi, lambda, cuts for n > TS
   size_t scratch_per_cta;
-  int* counter;
+  int* counter;          // [0]: large-instance queue, [1]: the rest
   int ts;                // tile bits
   int max_n;             // scratch is sized for this many qubits
   int* error;            // device error word (bit 1: malformed instance skipped)
 };
+
+namespace cg = cooperative_groups;
+
+// One instance, processed by `csize` CTAs of a cluster (csize == 1: this CTA
+// alone).  All CTAs of the group call it with the same idx.
+template <int LAY>
+__device__ void run_instance(const BatchParams& B, int idx, int crank, int csize, typename Types<LAY>::E* sp,
+                             typename Types<LAY>::E* sl, uint16_t* sc, Coef* tab, double* red, uint8_t* s_edges,
+                             double* part, char* scratch) {
+  using E = typename Types<LAY>::E;
+  const int TS = B.ts;
+  const int NT = 1 << TS;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const bool coop = csize > 1;
+  cg::cluster_group cluster = cg::this_cluster();
+  auto group_sync = [&]() {
+    if (coop) cluster.sync();
+    else __syncthreads();
+  };
+  __shared__ int s_bad;
+  const BatchInstanceDev I = B.inst[idx];
+  const int n = I.n, p = I.p, ne = I.nedges;
+  // a malformed instance is skipped: NaN outputs and the error word
+  if (tid == 0)
+    s_bad = n < 1 || n > B.max_n || n > 2 * TS || p < 0 || p > 64 || ne < 0 || ne > BATCH_MAX_EDGES;
+  __syncthreads();
+  for (int e = tid; e < 2 * ne && !s_bad; e += nthr)
+    if (B.edges[2 * I.edge_offset + e] >= n) s_bad = 1;
+  __syncthreads();
+  if (s_bad) {
+    if (tid == 0 && crank == 0) {
+      if (p >= 0 && p <= 64)
+        for (int k = 0; k <= 2 * p; ++k) B.out[I.out_offset + k] = __longlong_as_double(0x7ff8000000000000ll);
+      atomicOr(B.error, 2);
+    }
+    group_sync();
+    return;
+  }
+  const int64_t namps = int64_t(1) << n;
+  for (int e = tid; e < 2 * ne; e += nthr) s_edges[e] = (uint8_t)(n - 1 - B.edges[2 * I.edge_offset + e]);
+  __syncthreads();
+  const double* beta = B.angles + I.angle_offset;
+  const double* gamma = beta + p;
+  const float half_e = 0.5f * ne;
+  const bool small = n <= TS;
+  E* gp = reinterpret_cast<E*>(scratch);
+  E* gl = gp + namps;
+  uint16_t* gc = reinterpret_cast<uint16_t*>(gl + namps);
+
+  const E plus = [&] {
+    const double a = 1.0 / sqrt((double)namps);
+    if constexpr (LAY == C64) return make_float2((float)a, 0.f);
+    else {
+      float h, l;
+      split_d(a, h, l);
+      return make_float4(h, l, 0.f, 0.f);
+    }
+  }();
+  for (int64_t x = (int64_t)crank * nthr + tid; x < namps; x += (int64_t)csize * nthr) {
+    unsigned c = 0;
+    for (int e = 0; e < ne; ++e) c += (unsigned)(((x >> s_edges[2 * e]) ^ (x >> s_edges[2 * e + 1])) & 1);
+    if (small) {
+      sc[x] = (uint16_t)c;
+      sp[x] = plus;
+    } else {
+      gc[x] = (uint16_t)c;
+      gp[x] = plus;
+    }
+  }
+  group_sync();
+
+  const int hcount = small ? 0 : n - TS;
+  const int lowB = TS - hcount;
+  auto pass = [&](bool passA, const TileOpsB& T, const Coef& rc, const Coef& rs, FFAcc& ax, FFAcc& acut,
+                  FFAcc& ae) {
+    if (small) {
+      tile_apply_b<E>(T, sp, sl, sc, tab, rc, rs, half_e, ax, acut, ae);
+      return;
+    }
+    const int64_t ntile = int64_t(1) << (n - TS);
+    for (int64_t t = crank; t < ntile; t += csize) {
+      for (int l = tid; l < NT; l += nthr) {
+        int64_t x;
+        if (passA) x = (t << TS) | l;
+        else x = (int64_t(l >> lowB) << TS) | (t << lowB) | (l & ((1 << lowB) - 1));
+        sp[l] = gp[x];
+        if (T.dual && !T.init) sl[l] = gl[x];
+        sc[l] = gc[x];
+      }
+      __syncthreads();
+      tile_apply_b<E>(T, sp, sl, sc, tab, rc, rs, half_e, ax, acut, ae);
+      for (int l = tid; l < NT; l += nthr) {
+        int64_t x;
+        if (passA) x = (t << TS) | l;
+        else x = (int64_t(l >> lowB) << TS) | (t << lowB) | (l & ((1 << lowB) - 1));
+        gp[x] = sp[l];
+        if (T.dual) gl[x] = sl[l];
+      }
+      __syncthreads();
+    }
+    group_sync();
+  };
+  auto fill_phase = [&](double g, int sign) {
+    for (int c = tid; c <= ne; c += nthr) {
+      double sn, cs;
+      sincos(sign * g * (0.5 * ne - c), &sn, &cs);
+      tab[c] = coef_dev<LAY>(cs, sn);
+    }
+    __syncthreads();
+  };
+  auto rx_coefs = [&](double b, Coef& rc, Coef& rs) {
+    rc = coef_dev<LAY>(cos(0.5 * b), 0.0);
+    rs = coef_dev<LAY>(sin(0.5 * b), 0.0);
+  };
+  // sum of a per-CTA value over the group, delivered to rank 0
+  auto group_total = [&](double v, int slot) -> double {
+    if (!coop) return v;
+    if (tid == 0) part[slot] = v;
+    cluster.sync();
+    double s = 0.0;
+    if (crank == 0 && tid == 0)
+      for (int r = 0; r < csize; ++r) s += *cluster.map_shared_rank(&part[slot], r);
+    cluster.sync();
+    return s;
+  };
+
+  // ---- forward
+  FFAcc dummy;
+  dummy.zero();
+  for (int l = 0; l < p; ++l) {
+    fill_phase(gamma[l], +1);
+    Coef rc, rs;
+    rx_coefs(beta[l], rc, rs);
+    TileOpsB T{};
+    T.dir = 1;
+    T.dual = false;
+    if (small) {
+      T.tb = n;
+      T.phase = true;
+      T.nbits = n;
+      for (int b = 0; b < n; ++b) T.lbits[b] = b;
+      pass(true, T, rc, rs, dummy, dummy, dummy);
+    } else {
+      T.tb = TS;
+      T.phase = true;
+      T.nbits = TS;
+      for (int b = 0; b < TS; ++b) T.lbits[b] = b;
+      pass(true, T, rc, rs, dummy, dummy, dummy);
+      T.phase = false;
+      T.nbits = hcount;
+      for (int b = 0; b < hcount; ++b) T.lbits[b] = lowB + b;
+      pass(false, T, rc, rs, dummy, dummy, dummy);
+    }
+  }
+  // ---- backward (adjoint)
+  double* o = B.out + I.out_offset;
+  FFAcc ae;
+  ae.zero();
+  bool first = true;
+  for (int l = p - 1; l >= 0; --l) {
+    fill_phase(gamma[l], -1);
+    Coef rc, rs;
+    rx_coefs(-beta[l], rc, rs);
+    FFAcc ax, acut;
+    ax.zero();
+    acut.zero();
+    TileOpsB T{};
+    T.dir = -1;
+    T.dual = true;
+    if (small) {
+      T.tb = n;
+      T.init = first;
+      T.phase = true;
+      T.nbits = n;
+      for (int b = 0; b < n; ++b) T.lbits[b] = b;
+      pass(true, T, rc, rs, ax, acut, ae);
+    } else {
+      T.tb = TS;
+      T.init = first;
+      T.phase = false;
+      T.nbits = hcount;
+      for (int b = 0; b < hcount; ++b) T.lbits[b] = lowB + b;
+      pass(false, T, rc, rs, ax, acut, ae);
+      T.init = false;
+      T.phase = true;
+      T.nbits = TS;
+      for (int b = 0; b < TS; ++b) T.lbits[b] = b;
+      pass(true, T, rc, rs, ax, acut, ae);
+    }
+    first = false;
+    const double gx = group_total(block_sum(ax, red), 0);
+    const double gc2 = group_total(block_sum(acut, red), 1);
+    if (tid == 0 && crank == 0) {
+      o[p + l] = gx;
+      o[l] = -2.0 * gc2;
+    }
+  }
+  if (p == 0) {
+    for (int64_t x = (int64_t)crank * nthr + tid; x < namps; x += (int64_t)csize * nthr)
+      norm2acc(ae, small ? sp[x] : gp[x], (float)(small ? sc[x] : gc[x]));
+  }
+  const double e = group_total(block_sum(ae, red), 2);
+  if (tid == 0 && crank == 0) o[2 * p] = e;
+  __syncthreads();
+}
 
 template <int LAY>
 __global__ void __launch_bounds__(BATCH_THREADS) k_batch(const __grid_constant__ BatchParams B) {
@@ -233,194 +442,37 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch(const __grid_constant__
   uint16_t* sc = reinterpret_cast<uint16_t*>(sl + NT);
   Coef* tab = reinterpret_cast<Coef*>(sc + NT);  // BATCH_MAX_EDGES + 1 entries
   __shared__ double red[32];
-  __shared__ int s_inst;
+  __shared__ double part[4];
+  __shared__ int s_item;
   __shared__ uint8_t s_edges[2 * BATCH_MAX_EDGES];
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  E* gpsi = reinterpret_cast<E*>(B.scratch + (size_t)blockIdx.x * B.scratch_per_cta);
+  const int tid = threadIdx.x;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank();
+  const int csize = (int)cluster.num_blocks();
+  // the cluster leader's scratch slice holds a cooperative instance
+  const size_t cl_first = blockIdx.x - crank;
+  char* lead_scratch = B.scratch + cl_first * B.scratch_per_cta;
+  char* own_scratch = B.scratch + (size_t)blockIdx.x * B.scratch_per_cta;
 
+  // phase 1: large instances, one cluster each
+  if (B.nlarge > 0) {
+    for (;;) {
+      if (crank == 0 && tid == 0) s_item = atomicAdd(&B.counter[0], 1);
+      cluster.sync();
+      const int item = *cluster.map_shared_rank(&s_item, 0);
+      cluster.sync();
+      if (item >= B.nlarge) break;
+      run_instance<LAY>(B, item, crank, csize, sp, sl, sc, tab, red, s_edges, part, lead_scratch);
+    }
+  }
+  // phase 2: everything else, one CTA each
   for (;;) {
-    if (tid == 0) s_inst = atomicAdd(B.counter, 1);
+    if (tid == 0) s_item = B.nlarge + atomicAdd(&B.counter[1], 1);
     __syncthreads();
-    const int idx = s_inst;
+    const int idx = s_item;
     __syncthreads();
     if (idx >= B.ninst) break;
-    const BatchInstanceDev I = B.inst[idx];
-    const int n = I.n, p = I.p, ne = I.nedges;
-    // a malformed instance is skipped: NaN outputs and the error word
-    __shared__ int s_bad;
-    if (tid == 0)
-      s_bad = n < 1 || n > B.max_n || n > 2 * TS || p < 0 || p > 64 || ne < 0 || ne > BATCH_MAX_EDGES;
-    __syncthreads();
-    for (int e = tid; e < 2 * ne && !s_bad; e += nthr)
-      if (B.edges[2 * I.edge_offset + e] >= n) s_bad = 1;
-    __syncthreads();
-    if (s_bad) {
-      if (tid == 0) {
-        if (p >= 0 && p <= 64)
-          for (int k = 0; k <= 2 * p; ++k) B.out[I.out_offset + k] = __longlong_as_double(0x7ff8000000000000ll);
-        atomicOr(B.error, 2);
-      }
-      __syncthreads();
-      continue;
-    }
-    const int64_t namps = int64_t(1) << n;
-    for (int e = tid; e < 2 * ne; e += nthr) s_edges[e] = (uint8_t)(n - 1 - B.edges[2 * I.edge_offset + e]);
-    __syncthreads();
-    const double* beta = B.angles + I.angle_offset;
-    const double* gamma = beta + p;
-    const float half_e = 0.5f * ne;
-    const bool small = n <= TS;
-    // storage for psi, lambda, cuts
-    E* gp = gpsi;
-    E* gl = gpsi + namps;
-    uint16_t* gc = reinterpret_cast<uint16_t*>(gl + namps);
-
-    // cut table and |+>
-    const E plus = [&] {
-      const double a = 1.0 / sqrt((double)namps);
-      if constexpr (LAY == C64) return make_float2((float)a, 0.f);
-      else {
-        float h, l;
-        split_d(a, h, l);
-        return make_float4(h, l, 0.f, 0.f);
-      }
-    }();
-    for (int64_t x = tid; x < namps; x += nthr) {
-      unsigned c = 0;
-      for (int e = 0; e < ne; ++e) c += (unsigned)(((x >> s_edges[2 * e]) ^ (x >> s_edges[2 * e + 1])) & 1);
-      if (small) {
-        sc[x] = (uint16_t)c;
-        sp[x] = plus;
-      } else {
-        gc[x] = (uint16_t)c;
-        gp[x] = plus;
-      }
-    }
-    __syncthreads();
-
-    // tile geometry for large instances: pass A = bits [0, TS), pass B =
-    // bits [TS, n) plus the low bits [0, TS - (n - TS))
-    const int hcount = small ? 0 : n - TS;
-    const int lowB = TS - hcount;
-    auto pass = [&](bool passA, const TileOpsB& T, const Coef& rc, const Coef& rs, FFAcc& ax, FFAcc& acut,
-                    FFAcc& ae) {
-      if (small) {
-        tile_apply_b<E>(T, sp, sl, sc, tab, rc, rs, half_e, ax, acut, ae);
-        return;
-      }
-      const int64_t ntile = int64_t(1) << (n - TS);
-      for (int64_t t = 0; t < ntile; ++t) {
-        // load tile (coalesced): local index -> global index
-        for (int l = tid; l < NT; l += nthr) {
-          int64_t x;
-          if (passA) x = (t << TS) | l;
-          else x = (int64_t(l >> lowB) << TS) | (t << lowB) | (l & ((1 << lowB) - 1));
-          sp[l] = gp[x];
-          if (T.dual && !T.init) sl[l] = gl[x];
-          sc[l] = gc[x];
-        }
-        __syncthreads();
-        tile_apply_b<E>(T, sp, sl, sc, tab, rc, rs, half_e, ax, acut, ae);
-        for (int l = tid; l < NT; l += nthr) {
-          int64_t x;
-          if (passA) x = (t << TS) | l;
-          else x = (int64_t(l >> lowB) << TS) | (t << lowB) | (l & ((1 << lowB) - 1));
-          gp[x] = sp[l];
-          if (T.dual) gl[x] = sl[l];
-        }
-        __syncthreads();
-      }
-    };
-    auto fill_phase = [&](double g, int sign) {
-      for (int c = tid; c <= ne; c += nthr) {
-        double sn, cs;
-        sincos(sign * g * (0.5 * ne - c), &sn, &cs);
-        tab[c] = coef_dev<LAY>(cs, sn);
-      }
-      __syncthreads();
-    };
-    auto rx_coefs = [&](double b, Coef& rc, Coef& rs) {
-      rc = coef_dev<LAY>(cos(0.5 * b), 0.0);
-      rs = coef_dev<LAY>(sin(0.5 * b), 0.0);
-    };
-
-    // ---- forward
-    FFAcc dummy;
-    dummy.zero();
-    for (int l = 0; l < p; ++l) {
-      fill_phase(gamma[l], +1);
-      Coef rc, rs;
-      rx_coefs(beta[l], rc, rs);
-      TileOpsB T{};
-      T.dir = 1;
-      T.dual = false;
-      if (small) {
-        T.tb = n;
-        T.phase = true;
-        T.nbits = n;
-        for (int b = 0; b < n; ++b) T.lbits[b] = b;
-        pass(true, T, rc, rs, dummy, dummy, dummy);
-      } else {
-        T.tb = TS;
-        T.phase = true;
-        T.nbits = TS;
-        for (int b = 0; b < TS; ++b) T.lbits[b] = b;
-        pass(true, T, rc, rs, dummy, dummy, dummy);
-        T.phase = false;
-        T.nbits = hcount;
-        for (int b = 0; b < hcount; ++b) T.lbits[b] = lowB + b;
-        pass(false, T, rc, rs, dummy, dummy, dummy);
-      }
-    }
-    // ---- backward (adjoint)
-    double* o = B.out + I.out_offset;
-    FFAcc ae;
-    ae.zero();
-    bool first = true;
-    for (int l = p - 1; l >= 0; --l) {
-      fill_phase(gamma[l], -1);
-      Coef rc, rs;
-      rx_coefs(-beta[l], rc, rs);
-      FFAcc ax, acut;
-      ax.zero();
-      acut.zero();
-      TileOpsB T{};
-      T.dir = -1;
-      T.dual = true;
-      if (small) {
-        T.tb = n;
-        T.init = first;
-        T.phase = true;
-        T.nbits = n;
-        for (int b = 0; b < n; ++b) T.lbits[b] = b;
-        pass(true, T, rc, rs, ax, acut, ae);
-      } else {
-        T.tb = TS;
-        T.init = first;
-        T.phase = false;
-        T.nbits = hcount;
-        for (int b = 0; b < hcount; ++b) T.lbits[b] = lowB + b;
-        pass(false, T, rc, rs, ax, acut, ae);
-        T.init = false;
-        T.phase = true;
-        T.nbits = TS;
-        for (int b = 0; b < TS; ++b) T.lbits[b] = b;
-        pass(true, T, rc, rs, ax, acut, ae);
-      }
-      first = false;
-      const double gx = block_sum(ax, red);
-      const double gc2 = block_sum(acut, red);
-      if (tid == 0) {
-        o[p + l] = gx;
-        o[l] = -2.0 * gc2;
-      }
-    }
-    if (p == 0) {
-      for (int64_t x = tid; x < namps; x += nthr) norm2acc(ae, small ? sp[x] : gp[x], (float)(small ? sc[x] : gc[x]));
-    }
-    const double e = block_sum(ae, red);
-    if (tid == 0) o[2 * p] = e;
-    __syncthreads();
+    run_instance<LAY>(B, idx, 0, 1, sp, sl, sc, tab, red, s_edges, part, own_scratch);
   }
 }
 
@@ -437,7 +489,7 @@ size_t batch_workspace_bytes(int max_n, int layout, int ctas) {
 
 int* device_error_word();
 
-int batch_qaoa(const qf_batch_instance* inst, int ninst, const uint8_t* edges, const double* angles,
+int batch_qaoa(const qf_batch_instance* inst, int ninst, int nlarge, const uint8_t* edges, const double* angles,
                double* out, int layout, int max_n, int ts, int ctas, void* ws, size_t ws_bytes,
                cudaStream_t stream) {
   BatchParams B;
@@ -447,6 +499,7 @@ int batch_qaoa(const qf_batch_instance* inst, int ninst, const uint8_t* edges, c
   if (B.error == nullptr) return QF_ERR_CUDA;
   B.inst = reinterpret_cast<const BatchInstanceDev*>(inst);
   B.ninst = ninst;
+  B.nlarge = nlarge;
   B.edges = edges;
   B.angles = angles;
   B.out = out;
@@ -456,30 +509,36 @@ int batch_qaoa(const qf_batch_instance* inst, int ninst, const uint8_t* edges, c
   B.scratch_per_cta = ((amps * (2 * elem_bytes(layout) + 2)) + 255) & ~size_t(255);
   B.ts = ts;
   if (ws_bytes < batch_workspace_bytes(max_n, layout, ctas)) return QF_ERR_WORKSPACE;
-  int rc = check_cuda(cudaMemsetAsync(B.counter, 0, sizeof(int), stream));
+  int rc = check_cuda(cudaMemsetAsync(B.counter, 0, 2 * sizeof(int), stream));
   if (rc) return rc;
   const size_t smem = batch_smem_bytes(layout, ts);
   static std::atomic<bool> attr[2][64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (layout == C64) {
-    if (dev < 64 && !attr[0][dev].load()) {
-      rc = check_cuda(cudaFuncSetAttribute(k_batch<C64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      if (rc) return rc;
-      attr[0][dev].store(true);
-    }
-    k_batch<C64><<<ctas, BATCH_THREADS, smem, stream>>>(B);
-  } else if (layout == FF) {
-    if (dev < 64 && !attr[1][dev].load()) {
-      rc = check_cuda(cudaFuncSetAttribute(k_batch<FF>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-      if (rc) return rc;
-      attr[1][dev].store(true);
-    }
-    k_batch<FF><<<ctas, BATCH_THREADS, smem, stream>>>(B);
-  } else {
-    return QF_ERR_LAYOUT;
+  void (*kern)(BatchParams) = layout == C64 ? k_batch<C64> : k_batch<FF>;
+  const int li = layout == C64 ? 0 : 1;
+  if (layout != C64 && layout != FF) return QF_ERR_LAYOUT;
+  if (dev < 64 && !attr[li][dev].load()) {
+    rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    if (rc) return rc;
+    rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    if (rc) return rc;
+    attr[li][dev].store(true);
   }
-  return check_cuda(cudaGetLastError());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(BATCH_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = BATCH_CLUSTER;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  rc = check_cuda(cudaLaunchKernelEx(&cfg, kern, B));
+  return rc;
 }
 
 }  // namespace qf

@@ -17,7 +17,7 @@ int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, i
                const double* gamma, const double* node_theta, int fusion_k, cudaStream_t stream);
 size_t qaoa_grad_workspace_bytes(int n, int p, int layout);
 size_t batch_workspace_bytes(int max_n, int layout, int ctas);
-int batch_qaoa(const qf_batch_instance* inst, int ninst, const uint8_t* edges, const double* angles,
+int batch_qaoa(const qf_batch_instance* inst, int ninst, int nlarge, const uint8_t* edges, const double* angles,
                double* out, int layout, int max_n, int ts, int ctas, void* ws, size_t ws_bytes,
                cudaStream_t stream);
 int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
@@ -218,20 +218,21 @@ size_t qf_batch_workspace_bytes(int max_n, int layout, int ctas) {
   return batch_workspace_bytes(max_n, layout, ctas);
 }
 
-int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, const uint8_t* edges,
+int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, int nlarge, const uint8_t* edges,
                        const double* angles, double* out, int layout, int max_n, int tile_bits, int ctas,
                        void* workspace, size_t workspace_bytes, void* stream) {
   if (layout != C64 && layout != FF) return QF_ERR_LAYOUT;
   if (ninstances < 0 || (ninstances > 0 && (instances == nullptr || angles == nullptr || out == nullptr)))
     return QF_ERR_INVALID_ARGUMENT;
-  if (max_n < 1 || max_n > 26 || ctas < 1 || ctas > 65535) return QF_ERR_INVALID_ARGUMENT;
+  if (nlarge < 0 || nlarge > ninstances) return QF_ERR_INVALID_ARGUMENT;
+  if (max_n < 1 || max_n > 26 || ctas < 8 || ctas > 65535 || ctas % 8 != 0) return QF_ERR_INVALID_ARGUMENT;
   const int ts_max = layout == C64 ? 12 : 11;
   if (tile_bits < 8 || tile_bits > ts_max || max_n > 2 * tile_bits) return QF_ERR_INVALID_ARGUMENT;
   int rc = check_ws(workspace, workspace_bytes, batch_workspace_bytes(max_n, layout, ctas));
   if (rc) return rc;
   if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
   if (ninstances == 0) return QF_OK;
-  return batch_qaoa(instances, ninstances, edges, angles, out, layout, max_n, tile_bits, ctas, workspace,
+  return batch_qaoa(instances, ninstances, nlarge, edges, angles, out, layout, max_n, tile_bits, ctas, workspace,
                     workspace_bytes, as_stream(stream));
 }
 

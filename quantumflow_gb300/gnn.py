@@ -52,9 +52,6 @@ class GraphBatch:
         self.adj = t(adj)
         self.device = device
 
-    def subset(self, idx):
-        raise NotImplementedError
-
 
 class AngleGNN:
     """The angle network with its parameters on the GPU."""
@@ -128,20 +125,18 @@ class AngleGNN:
         rng = np.random.default_rng(seed)
         labels = np.asarray(labels, dtype=np.float32)
         graphs = list(graphs)
-        order_batches = []
+        nb = (len(graphs) + batch_size - 1) // batch_size
+        cached = []  # four shuffles are built once and cycled (CSR building is host work)
         hist = []
         for ep in range(epochs):
-            perm = rng.permutation(len(graphs))
+            if ep < 4:
+                perm = rng.permutation(len(graphs))
+                cached.append([(perm[s:s + batch_size],
+                                GraphBatch([graphs[i] for i in perm[s:s + batch_size]], self.device))
+                               for s in range(0, len(graphs), batch_size)])
             tot, cnt = 0.0, 0
-            for s in range(0, len(graphs), batch_size):
-                idx = perm[s:s + batch_size]
-                key = (ep % 4, s)  # a few cached shuffles keep CSR building cheap
-                if ep < 4:
-                    b = GraphBatch([graphs[i] for i in idx], self.device)
-                    order_batches.append((idx, b))
-                else:
-                    idx, b = order_batches[(ep % 4) * ((len(graphs) + batch_size - 1) // batch_size)
-                                           + s // batch_size]
+            for k in range(nb):
+                idx, b = cached[ep % 4][k]
                 loss, grad = self.gradient(b, torch.from_numpy(labels[idx]))
                 self.adam_step(grad, lr=lr)
                 tot += float(loss) * len(idx)
@@ -174,7 +169,7 @@ def make_labels(graphs, p=6, steps=200, lr=0.05, dtype="complex64", init=None):
     else:
         betas, gammas = init
     batch.set_angles(betas, gammas)
-    batch.adam(steps, lr=lr, use_graph=True)
+    batch.optimize(steps, lr=lr)
     es, _, _ = batch.evaluate()
     betas, gammas = batch.get_angles()
     return np.concatenate([np.stack(betas), np.stack(gammas)], axis=1), es

@@ -44,7 +44,7 @@ def test_batch_matches_single_instance(dtype, tol):
     assert nat.device_error() == 0
 
 
-@pytest.mark.parametrize("tile_bits", [8, 10])
+@pytest.mark.parametrize("tile_bits", [8, 9, 10])
 def test_batch_large_instances_tiled(tile_bits):
     """Instances above the tile size run the global-scratch tiled passes."""
     import quantumflow_gb300 as qf
@@ -53,7 +53,8 @@ def test_batch_large_instances_tiled(tile_bits):
     ps = [3, 2, 2, 4]
     betas = [rng.uniform(0, np.pi, p) for p in ps]
     gammas = [rng.uniform(0, np.pi, p) for p in ps]
-    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128", tile_bits=tile_bits, ctas=8)
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128", tile_bits=tile_bits, ctas=16)
+    assert batch.nlarge == sum(n >= tile_bits + 4 for n in (12, 14, 16, 10))
     batch.set_angles(betas, gammas)
     es, dbs, dgs = batch.evaluate()
     for i, g in enumerate(graphs):
