@@ -140,6 +140,41 @@ def cpu_oracle_rate(ops, N, budget_s=12.0):
     return done * 2 * 16 * 2 ** N / dt / 1e9, done, dt
 
 
+def qaoa_time_to_ratio(args):
+    """Second half of the metric: QAOA MAXCUT, n=20, p=6, on seeded random
+    3-regular graphs, wall time until every graph has <C>/max C >= 0.90:
+    plain linear-ramp start with per-graph adjoint gradients, against the
+    learned start (network inference included) with batched adjoint
+    gradients.  Adam, lr 0.05, complex64."""
+    import torch
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import learned_init as li
+    if not os.path.exists(li.WEIGHTS):
+        return {"unavailable": "angle network weights missing"}
+    net = qf.gnn.AngleGNN.load(li.WEIGHTS)
+    rng = np.random.default_rng(20)
+    graphs = [qf.qaoa.random_regular_graph(3, 20, seed=int(rng.integers(1 << 30))) for _ in range(args.qaoa_graphs)]
+    li.time_to_ratio(net, graphs[:2], p=6, target=0.9, max_steps=20)  # warm-up (kernel attributes, caches)
+    torch.cuda.synchronize()
+    res = li.time_to_ratio(net, graphs, p=6, target=0.9, max_steps=400)
+    mc = li.max_cuts(graphs)
+    b, g = qf.qaoa.linear_ramp_angles(6)
+    betas, gammas = qf.gnn.predict_angles(net, graphs)
+    init_plain = float(np.mean([qf.QAOAMaxCut(gr, 6, dtype="complex64").expectation(b, g) / m
+                                for gr, m in zip(graphs, mc)]))
+    init_learned = float(np.mean([qf.QAOAMaxCut(gr, 6, dtype="complex64").expectation(bb, gg) / m
+                                  for gr, m, bb, gg in zip(graphs, mc, betas, gammas)]))
+    plain_s = res["plain_single"]["seconds"]
+    learned_s = res["learned_batched"]["seconds"]
+    return {"workload": f"{len(graphs)} random 3-regular graphs, n=20, p=6, target ratio 0.90, complex64",
+            "plain_init_single_s": plain_s, "plain_init_batched_s": res["plain_batched"]["seconds"],
+            "learned_init_batched_s": learned_s, "speedup_learned_batched_vs_plain_single": plain_s / learned_s,
+            "initial_ratio_plain": init_plain, "initial_ratio_learned": init_learned,
+            "mean_steps_plain": res["plain_single"]["mean_steps"],
+            "mean_steps_learned": res["learned_batched"]["mean_steps"],
+            "reached": {k: res[k]["reached"] for k in ("plain_single", "plain_batched", "learned_batched")}}
+
+
 def run_reference(args, rank, world):
     """Reference arm: the CPU oracle port (the reference is pure Python; its
     numpy backend's tensormul is np.einsum, restated in oracle/qf_oracle.py)."""
@@ -191,6 +226,8 @@ def main():
     ap.add_argument("--fusion", type=int, default=0, help="0 = library default per element type")
     ap.add_argument("--seed", type=int, default=2018)
     ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
+    ap.add_argument("--no-qaoa", action="store_true", help="skip the QAOA time-to-ratio measurement")
+    ap.add_argument("--qaoa-graphs", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-n", type=int, default=28)
@@ -310,6 +347,10 @@ def main():
                "ms_per_step": ems, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
         del host_in, host_out
 
+    qaoa = None
+    if not args.no_qaoa and rank == 0:
+        qaoa = qaoa_time_to_ratio(args)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         cpu_ops = c2_circuit_ops(args.cpu_n, 1, args.seed)
@@ -337,6 +378,7 @@ def main():
             "pass_gbs": world * passes * sweep_bytes / (ms * 1e-3) / 1e9,
             "roofline": roofline,
             "kernel_ms_per_step": {k: m / args.steps for k, (m, c) in kt.items() if c},
+            "qaoa": qaoa,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clock_info,
