@@ -62,6 +62,15 @@ def build_circuit(ops):
     return circ
 
 
+def warp_traffic(N, S):
+    """DRAM bytes per fused-pass launch: read + write measured by ncu on the
+    same kernel at N=24 complex128 (268.6 MB + 207.2 MB; the write shortfall
+    is dirty L2 at kernel end), scaled by the state size to N qubits."""
+    if S != 16:
+        return None
+    return (268.558592e6 + 207.177984e6) * 2 ** (N - 24)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -305,7 +314,31 @@ def main():
     value = world * ngates * sweep_bytes / (ms * 1e-3) / 1e9
     launches = sum(c for _, c in kt.values()) + args.steps  # + one |0> fill per step
 
+    # unfused 2x2 sweeps on every qubit (the plain gate-sweep kernel) under
+    # the same per-launch CUDA-event timing
+    sweep = None
+    if rank == 0:
+        sweep_circ = build_circuit([op for op in ops[:N] if op[0] == 1])
+        ket = sweep_circ.run(qf.zero_state(N, dtype=args.dtype), fusion_k=1)
+        del ket
+        torch.cuda.synchronize()
+        nat.timing_collect()
+        nat.timing_enable(True)
+        for _ in range(2):
+            ket = sweep_circ.run(qf.zero_state(N, dtype=args.dtype), fusion_k=1)
+            del ket
+        torch.cuda.synchronize()
+        nat.timing_enable(False)
+        sk = nat.timing_collect()
+        sms, scount = sk["dense1"]
+        if scount:
+            sweep_ach = sweep_bytes / (sms / scount * 1e-3) / 1e9
+            sweep = {"kernel": "k_dense1 (one 2x2 gate per pass, all 28 qubits)", "achieved": sweep_ach,
+                     "peak": None, "unit": "GB/s", "frac": None, "launches_timed": scount}
+
     peak, peak_kind = measured_peaks()
+    if sweep is not None:
+        sweep["peak"], sweep["frac"] = peak, sweep["achieved"] / peak
     dom = max(kt, key=lambda k: kt[k][0])
     dom_ms, dom_n = kt[dom]
     achieved = sweep_bytes / (dom_ms / dom_n * 1e-3) / 1e9 if dom_n else None
@@ -313,7 +346,7 @@ def main():
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
         "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-        "traffic": None, "launches_timed": dom_n,
+        "traffic": warp_traffic(N, S) if dom == "warp_tile" else None, "launches_timed": dom_n,
         "share_of_kernel_time": dom_ms / total_kernel_ms if total_kernel_ms else None,
         "bytes_per_launch": sweep_bytes,
     }
@@ -377,6 +410,7 @@ def main():
             "passes_per_step": passes,
             "pass_gbs": world * passes * sweep_bytes / (ms * 1e-3) / 1e9,
             "roofline": roofline,
+            "sweep_roofline": sweep,
             "kernel_ms_per_step": {k: m / args.steps for k, (m, c) in kt.items() if c},
             "qaoa": qaoa,
             "cpu_baseline": cpu,
