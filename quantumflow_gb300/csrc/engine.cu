@@ -746,6 +746,32 @@ __global__ void __launch_bounds__(256) k_tile2(const __grid_constant__ TileParam
 }
 
 // -------------------------------------------------------------- k_warp ----
+// Exchange register-index bits J and K: a register permutation (moves only).
+template <int RB, int J, int K, typename E>
+QF_D void rswap(E (&a)[1 << RB]) {
+#pragma unroll
+  for (int r = 0; r < (1 << RB); ++r) {
+    const int bj = (r >> J) & 1, bk = (r >> K) & 1;
+    if (bj == 0 && bk == 1) {
+      const int q = r ^ (1 << J) ^ (1 << K);
+      const E t = a[r];
+      a[r] = a[q];
+      a[q] = t;
+    }
+  }
+}
+template <int RB, typename E>
+QF_D void rswap_dispatch(int j, int k, E (&a)[1 << RB]) {
+  switch (j * 4 + k) {
+    case 1: rswap<RB, 0, 1>(a); break;
+    case 2: if constexpr (RB > 2) rswap<RB, 0, 2>(a); break;
+    case 3: if constexpr (RB > 3) rswap<RB, 0, 3>(a); break;
+    case 6: if constexpr (RB > 2) rswap<RB, 1, 2>(a); break;
+    case 7: if constexpr (RB > 3) rswap<RB, 1, 3>(a); break;
+    case 11: if constexpr (RB > 3) rswap<RB, 2, 3>(a); break;
+  }
+}
+
 template <int RB, typename E>
 QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t xb,
                       const int64_t (&hoff)[1 << RB], E (&a)[1 << RB]) {
@@ -780,7 +806,11 @@ QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, 
   }
 }
 
-template <int LAY, int RB>
+// SWAP = true: every register-bit gate runs one code variant on the top
+// register bit and the host inserts register-bit exchanges (small code,
+// for the long float-float gate bodies); SWAP = false: one variant per
+// register bit (no exchanges; for the short FP32 bodies).
+template <int LAY, int RB, bool SWAP>
 __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams P) {
   using E = typename Types<LAY>::E;
   constexpr int R = 1 << RB;
@@ -791,44 +821,63 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
   const int lane = threadIdx.x & 31;
   const int64_t nsub = int64_t(1) << (P.n - 5 - RB);
   const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
-  int64_t hoff[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    int64_t o = 0;
-#pragma unroll
-    for (int j = 0; j < RB; ++j)
-      if ((r >> j) & 1) o |= int64_t(1) << P.hb[j];
-    hoff[r] = o;
-  }
   const E* gin = reinterpret_cast<const E*>(P.in);
   E* gout = reinterpret_cast<E*>(P.out);
+  const uint32_t pb0 = (uint32_t)P.hb[0] | ((uint32_t)P.hb[1] << 8) | ((uint32_t)P.hb[2] << 16) |
+                       ((uint32_t)P.hb[3] << 24);
   for (int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); st < nsub; st += wstride) {
     int64_t base = st << 5;
 #pragma unroll
     for (int j = 0; j < RB; ++j) base = insert0(base, P.hb[j]);
     const int64_t xb = base | lane;
+    // register-index bit j holds global bit (pb >> 8j) & 255
+    uint32_t pb = pb0;
+    auto offset = [&](int r) {
+      int64_t o = 0;
+#pragma unroll
+      for (int j = 0; j < RB; ++j)
+        if ((r >> j) & 1) o |= int64_t(1) << ((pb >> (8 * j)) & 255u);
+      return o;
+    };
     E a[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[r] = gin[xb | hoff[r]];
+    for (int r = 0; r < R; ++r) a[r] = gin[xb | offset(r)];
     for (int pc = 0; pc < P.nprog; ++pc) {
       const TInstr in = P.prog[pc];
       switch (in.code) {
         case I_G1R:
-          g1_reg_dispatch<RB>(in.a, &P.coef[in.coef], a);
+          if constexpr (SWAP) g1_reg<RB, RB - 1>(&P.coef[in.coef], a);
+          else g1_reg_dispatch<RB>(in.a, &P.coef[in.coef], a);
           break;
         case I_G1L:
           g1_lane<RB>(in.a, &P.coef[in.coef], a, lane);
           break;
         case I_G2R:
-          g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
+          if constexpr (SWAP) {
+            if constexpr (RB >= 2) g2_reg<RB, RB - 1, RB - 2>(&P.coef[in.coef], a);
+          } else {
+            g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
+          }
           break;
-        case I_SEG:
+        case I_RSWAP:
+          if constexpr (SWAP) {
+            rswap_dispatch<RB>(in.a, in.b, a);
+            const uint32_t sa = 8u * in.a, sb = 8u * in.b;
+            const uint32_t va = (pb >> sa) & 255u, vb = (pb >> sb) & 255u;
+            pb = (pb & ~((255u << sa) | (255u << sb))) | (vb << sa) | (va << sb);
+          }
+          break;
+        case I_SEG: {
+          int64_t hoff[R];
+#pragma unroll
+          for (int r = 0; r < R; ++r) hoff[r] = offset(r);
           seg_apply_w<RB>(P, in, scoef, xb, hoff, a);
           break;
+        }
       }
     }
 #pragma unroll
-    for (int r = 0; r < R; ++r) gout[xb | hoff[r]] = a[r];
+    for (int r = 0; r < R; ++r) gout[xb | offset(r)] = a[r];
   }
 }
 
@@ -1365,6 +1414,7 @@ template <int LAY, int RB>
 static int launch_warp_t(const void* in, void* out, int n, const std::vector<HostOp>& ops,
                          const std::vector<int>& idx, cudaStream_t stream) {
   using E = typename Types<LAY>::E;
+  constexpr bool SWAP = LAY != C64;
   if (n < 5 + RB) return QF_ERR_NOT_SUPPORTED;
   static thread_local WarpParams P;
   std::memset(&P, 0, sizeof(P));
@@ -1388,6 +1438,9 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
   std::sort(hb.begin(), hb.end());
   for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];
   auto reg_of = [&](int b) { return (int)(std::find(hb.begin(), hb.end(), b) - hb.begin()); };
+  // pos[h]: register-index bit currently holding hb[h]; swaps bring a
+  // gate's bit to the top register bit (and a 2-qubit gate's LSB below it)
+  int pos[4] = {0, 1, 2, 3}, at[4] = {0, 1, 2, 3};
   // element-wise coefficients first (staged in shared memory), then dense
   int nc = 0, nprog = 0, nseg = 0;
   std::vector<int> coef_at(idx.size(), 0);
@@ -1442,29 +1495,50 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
         P.prog[nprog++] = TInstr{I_SEG, (uint8_t)nseg, 1, 0, 0, 0};
       }
       ++nseg;
-    } else if (op.type == OP_DENSE1) {
-      const int b = op.gb[0];
-      if (b < 5) P.prog[nprog++] = TInstr{I_G1L, (uint8_t)b, 0, 0, (uint16_t)coef_at[i], 0};
-      else P.prog[nprog++] = TInstr{I_G1R, (uint8_t)reg_of(b), 0, 0, (uint16_t)coef_at[i], 0};
     } else {
-      P.prog[nprog++] = TInstr{I_G2R, (uint8_t)reg_of(op.gb[0]), (uint8_t)reg_of(op.gb[1]), 0,
-                               (uint16_t)coef_at[i], 0};
+      auto bring = [&](int h, int target) -> bool {  // move hb[h] to register bit `target`
+        const int j = pos[h];
+        if (!SWAP || j == target) return true;
+        if (nprog >= 159) return false;
+        const int lo = j < target ? j : target, hi = j < target ? target : j;
+        P.prog[nprog++] = TInstr{I_RSWAP, (uint8_t)lo, (uint8_t)hi, 0, 0, 0};
+        const int other = at[target];
+        at[target] = h;
+        at[j] = other;
+        pos[h] = target;
+        pos[other] = j;
+        return true;
+      };
+      if (op.type == OP_DENSE1) {
+        const int b = op.gb[0];
+        if (b < 5) {
+          P.prog[nprog++] = TInstr{I_G1L, (uint8_t)b, 0, 0, (uint16_t)coef_at[i], 0};
+        } else {
+          if (!bring(reg_of(b), RB - 1)) return QF_ERR_NOT_SUPPORTED;
+          P.prog[nprog++] = TInstr{I_G1R, (uint8_t)(SWAP ? 0 : reg_of(b)), 0, 0, (uint16_t)coef_at[i], 0};
+        }
+      } else {
+        if (RB < 2) return QF_ERR_NOT_SUPPORTED;
+        if (!bring(reg_of(op.gb[0]), RB - 1) || !bring(reg_of(op.gb[1]), RB - 2)) return QF_ERR_NOT_SUPPORTED;
+        P.prog[nprog++] = TInstr{I_G2R, (uint8_t)(SWAP ? 0 : reg_of(op.gb[0])),
+                                 (uint8_t)(SWAP ? 0 : reg_of(op.gb[1])), 0, (uint16_t)coef_at[i], 0};
+      }
     }
   }
   P.nprog = nprog;
   const size_t smem = (size_t)P.necoef * sizeof(Coef);
   static std::atomic<bool> attr[64];
-  int rc = set_smem_attr(k_warp<LAY, RB>, attr);
+  int rc = set_smem_attr(k_warp<LAY, RB, SWAP>, attr);
   if (rc) return rc;
   const int64_t nsub = int64_t(1) << (n - 5 - RB);
   int64_t grid = (nsub + 7) / 8;
   const int64_t cap = (int64_t)device_sm_count() * 4;
   if (grid > cap) grid = cap;
-  k_warp<LAY, RB><<<(int)grid, 256, smem, stream>>>(P);
+  k_warp<LAY, RB, SWAP><<<(int)grid, 256, smem, stream>>>(P);
   return check_cuda(cudaGetLastError());
 }
 
-int warp_rb(int layout) { return layout == C64 ? 4 : 3; }
+int warp_rb(int layout) { return layout == C64 ? 4 : 2; }
 
 int launch_warp_block(const void* in, void* out, int n, int layout, const std::vector<HostOp>& ops,
                       const std::vector<int>& idx, int rb, cudaStream_t stream) {
@@ -1497,7 +1571,7 @@ int launch_tile_block(const void* in, void* out, int n, int layout, const std::v
 // Greedy fusion: walk the ops in order; element-wise ops join the current
 // block unconditionally (they need no tile bits), every other op joins while
 // the union of high bits (>= Lmin) stays within fusion_k.
-int g_default_fusion[3] = {4, 3, 3};  // per layout (C64, C128, FF): warp-tile capacity
+int g_default_fusion[3] = {4, 2, 2};  // per layout (C64, C128, FF): warp-tile capacity
 
 int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
             cudaStream_t stream, int* passes_out) {

@@ -51,6 +51,7 @@ enum TInstrCode : uint8_t {
   I_G2R = 4,   // a: register bit of the matrix MSB, b: of the LSB; 16 coefs
   I_SEG = 5,   // a: first SegOp, b: count (element-wise ops in registers)
   I_SMEM = 6,  // a: index into ops[] -- applied in shared memory
+  I_RSWAP = 7, // a, b: exchange register-index bits a and b (k_warp)
 };
 struct TInstr {
   uint8_t code, a, b, c;
