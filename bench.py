@@ -175,13 +175,25 @@ def qaoa_time_to_ratio(args):
                                   for gr, m, bb, gg in zip(graphs, mc, betas, gammas)]))
     plain_s = res["plain_single"]["seconds"]
     learned_s = res["learned_batched"]["seconds"]
+    # adjoint gradient throughput, random 3-regular n=24, p=8, complex128
+    g24 = qf.qaoa.random_regular_graph(3, 24, seed=24)
+    prob24 = qf.QAOAMaxCut(g24, 8)
+    b24, g24a = rng.uniform(0, np.pi, 8), rng.uniform(0, np.pi, 8)
+    prob24.expectation_and_grad(b24, g24a)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        prob24.expectation_and_grad(b24, g24a)
+    grad_rate = reps / (time.perf_counter() - t0)
     return {"workload": f"{len(graphs)} random 3-regular graphs, n=20, p=6, target ratio 0.90, complex64",
             "plain_init_single_s": plain_s, "plain_init_batched_s": res["plain_batched"]["seconds"],
             "learned_init_batched_s": learned_s, "speedup_learned_batched_vs_plain_single": plain_s / learned_s,
             "initial_ratio_plain": init_plain, "initial_ratio_learned": init_learned,
             "mean_steps_plain": res["plain_single"]["mean_steps"],
             "mean_steps_learned": res["learned_batched"]["mean_steps"],
-            "reached": {k: res[k]["reached"] for k in ("plain_single", "plain_batched", "learned_batched")}}
+            "reached": {k: res[k]["reached"] for k in ("plain_single", "plain_batched", "learned_batched")},
+            "adjoint_grad_evals_per_s_n24_p8_c128": grad_rate}
 
 
 def run_reference(args, rank, world):

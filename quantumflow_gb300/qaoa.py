@@ -246,10 +246,9 @@ class QAOAMaxCut:
         """(<C>, d<C>/d beta, d<C>/d gamma) by the adjoint method
         (qf_qaoa_expectation_grad): one forward sweep, then every layer undone
         on psi and lambda = C psi; two state vectors whatever p is."""
-        if not self.unweighted:
-            raise NotImplementedError("adjoint gradient needs an unweighted graph "
-                                      "(node weights are supported)")
         p = self.p
+        if not self.unweighted:
+            return self._weighted_grad(beta, gamma)
         beta = np.ascontiguousarray(beta, dtype=np.float64)
         gamma = np.ascontiguousarray(gamma, dtype=np.float64)
         if beta.shape != (p,) or gamma.shape != (p,):
@@ -268,6 +267,31 @@ class QAOAMaxCut:
                  int(self.fusion_k), nat.ptr(out), nat.ptr(ws), nbytes, nat.stream_handle(self.device))
         o = out.cpu().numpy()
         return float(o[2 * p]), o[p:2 * p].copy(), o[:p].copy()
+
+
+def _weighted_grad_impl(prob, beta, gamma):
+    """Weighted edges: the generic circuit adjoint over qubo_circuit, with the
+    chain rule for the shared angles (ZZ(t), t = -w gamma / pi; RX(beta))."""
+    from .adjoint import expectation_and_grad
+    circ = prob.circuit(beta, gamma)
+    e, grads = expectation_and_grad(circ, prob.cuts, dtype=prob.dtype)
+    p = prob.p
+    gb, gg = np.zeros(p), np.zeros(p)
+    nodes = list(prob.graph.nodes())
+    weighted_nodes = sum(1 for q in nodes if prob.graph.nodes[q].get("weight", None) is not None)
+    k = len(nodes)  # the H layer
+    for l in range(p):
+        for w in prob.weights:
+            gg[l] += grads.get((k, "t"), 0.0) * (-w / np.pi)
+            k += 1
+        k += weighted_nodes
+        for _ in nodes:
+            gb[l] += grads.get((k, "theta"), 0.0)
+            k += 1
+    return e, gb, gg
+
+
+QAOAMaxCut._weighted_grad = lambda self, beta, gamma: _weighted_grad_impl(self, beta, gamma)
 
 
 class QAOAExpectation(torch.autograd.Function):

