@@ -83,8 +83,10 @@ int qf_timing_enable(int on);
 /* Fused-pass kernel selection (diagnostics and tests; no reference
  * counterpart), process-wide: 0 = default (warp tiles, then shared-memory
  * register programs, then the shared-memory kernel, whichever first fits
- * the block); 1 = shared-memory kernel only; 2, 3, 4 = default order with
- * warp tiles of 2^mode registers per thread. */
+ * the block); 1 = shared-memory kernels only (gate passes and the QAOA
+ * adjoint); 2, 3, 4 = default order with warp tiles of 2^mode registers per
+ * thread (the adjoint's warp tiles take 2 or 3 for complex128 and
+ * float-float, 3 or 4 for complex64, else their default). */
 int qf_set_tile_kernel(int mode);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
 

@@ -123,6 +123,17 @@ QF_D void acc_imconj(FFAcc& acc, double2 l, double2 p, float w) {
   acc_imconj(acc, to_ff(l), to_ff(p), w);
 }
 
+
+QF_D float2 shfl_xor_e(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+QF_D double2 shfl_xor_e(double2 v, int m) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+QF_D float4 shfl_xor_e(float4 v, int m) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
+}
 QF_D int64_t adj_global(const AdjParams& P, int64_t base, int l) {
   int64_t x = base | (l & ((1 << P.L) - 1));
   for (int r = 0; r < P.nh; ++r)
@@ -317,16 +328,254 @@ __global__ void __launch_bounds__(256) k_adj(const __grid_constant__ AdjParams P
   }
 }
 
-__global__ void k_rows_sum(const double* rows, int nrows, int nslots, double* out) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += gridDim.x * blockDim.x) {
-    double v = 0.0;
-    for (int r = 0; r < nrows; ++r) v += rows[(size_t)r * nslots + s];
-    out[s] = v;
+// ------------------------------------------------- warp-tile adjoint ----
+// The same passes as k_adj with psi and lambda held in registers: a warp
+// owns a sub-tile of 32 lanes (global bits 0..4) x 2^RB registers (the
+// pass's high bits), gates on lane bits use shuffles, and nothing waits on
+// another warp.  The pass structure is fixed by the QAOA layer: optionally
+// lambda = C psi (the sweep's first pass), the mixer on the lane bits (a
+// layer's first pass) and on up to RB register bits, and the cost layer (a
+// layer's last pass).  Each sub-tile is prefetched two sub-tiles ahead into
+// a per-warp shared-memory ring with per-thread async copies.
+constexpr int ADJW_MAX_COEF = 1100;
+constexpr int ADJW_STAGES = 3;  // per-warp prefetch ring depth (sub-tiles)
+
+struct AdjWParams {
+  void* psi;
+  void* lam;
+  const uint16_t* cuts;
+  double* rows;
+  int32_t n, nslots;
+  int32_t init;   // lambda = c psi; <C> accumulator += c |psi|^2
+  int32_t lanes;  // mixer reduction + RX(-beta) on lane bits 0..4
+  int32_t nact;   // ... and on register bits 0..nact-1
+  int32_t last;   // cut reduction, node phases (ndiag), cut phase (ncut entries)
+  int32_t ndiag, ncut;
+  int32_t slot_x, slot_cut, slot_e;  // output slots of the three accumulators (-1: unused)
+  float wref;                        // E/2
+  uint8_t hb[4];                     // global bit of each register index bit
+  uint8_t hs[4];                     // the same bits in ascending order
+  uint8_t diag_bit[QF_MAX_QUBITS];   // global bit of each node phase
+  Coef rx_c, rx_s;                   // RX(-beta) = [[c, i s], [i s, c]]
+  Coef coef[ADJW_MAX_COEF];          // node phase pairs, then the cut table
+};
+
+// float-float a*x + b*y: both products exact to 2^-48, one TwoSum, one
+// renormalisation
+QF_D void ff_dot2(float ah, float al, float xh, float xl, float bh, float bl, float yh, float yl, float& rh,
+                  float& rl) {
+  float p0, c0, p1, c1, s, t;
+  ff_term(ah, al, xh, xl, p0, c0);
+  ff_term(bh, bl, yh, yl, p1, c1);
+  two_sum(p0, p1, s, t);
+  fast_two_sum(s, __fadd_rn(__fadd_rn(c0, c1), t), rh, rl);
+}
+// c a + i s p for real c, s (RX(-beta) row applied to self a and partner p)
+QF_D float4 rx_one(const Coef& c, const Coef& s, float4 a, float4 p) {
+  float4 o;
+  ff_dot2(c.f[0], c.f[1], a.x, a.y, -s.f[0], -s.f[1], p.z, p.w, o.x, o.y);
+  ff_dot2(c.f[0], c.f[1], a.z, a.w, s.f[0], s.f[1], p.x, p.y, o.z, o.w);
+  return o;
+}
+QF_D double2 rx_one(const Coef& c, const Coef& s, double2 a, double2 p) {
+  return make_double2(fma(c.d[0], a.x, -s.d[0] * p.y), fma(c.d[0], a.y, s.d[0] * p.x));
+}
+QF_D float2 rx_one(const Coef& c, const Coef& s, float2 a, float2 p) {
+  return make_float2(fmaf(c.f[0], a.x, -s.f[0] * p.y), fmaf(c.f[0], a.y, s.f[0] * p.x));
+}
+// acc += Im(conj(l) p)
+QF_D void redx_acc(FFAcc& acc, float4 l, float4 p) {
+  acc.add_prod(l.x, l.y, p.z, p.w);
+  acc.add_prod(-l.z, -l.w, p.x, p.y);
+}
+QF_D void redx_acc(FFAcc& acc, double2 l, double2 p) { acc_imconj(acc, l, p, 1.f); }
+QF_D void redx_acc(FFAcc& acc, float2 l, float2 p) {
+  acc.add_prod(l.x, 0.f, p.y, 0.f);
+  acc.add_prod(-l.y, 0.f, p.x, 0.f);
+}
+
+template <int LAY, int RB>
+constexpr size_t adjw_ring_bytes() {
+  return (size_t)8 * ADJW_STAGES * 2 * (32 << RB) * sizeof(typename Types<LAY>::E);
+}
+
+template <int LAY, int RB>
+__global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams P) {
+  using E = typename Types<LAY>::E;
+  constexpr int R = 1 << RB;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Coef* scoef = reinterpret_cast<Coef*>(smem_raw);
+  __shared__ double red[8][3];
+  const int necoef = 2 * P.ndiag + P.ncut;
+  for (int i = threadIdx.x; i < necoef; i += blockDim.x) scoef[i] = P.coef[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // this warp's ring: [stage][vector][register][lane]
+  E* ring = reinterpret_cast<E*>(smem_raw + (((size_t)necoef * sizeof(Coef) + 127) & ~size_t(127))) +
+            (size_t)warp * ADJW_STAGES * 2 * R * 32;
+  const int64_t nsub = int64_t(1) << (P.n - 5 - RB);
+  const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
+  E* gp = reinterpret_cast<E*>(P.psi);
+  E* gl = reinterpret_cast<E*>(P.lam);
+  const bool load_lambda = !P.init;
+  int64_t hoff[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    int64_t o = 0;
+#pragma unroll
+    for (int j = 0; j < RB; ++j)
+      if ((r >> j) & 1) o |= int64_t(1) << P.hb[j];
+    hoff[r] = o;
   }
+  auto sub_base = [&](int64_t st) {
+    int64_t base = st << 5;
+#pragma unroll
+    for (int j = 0; j < RB; ++j) base = insert0(base, P.hs[j]);
+    return base | lane;
+  };
+  // prefetch sub-tile st into ring stage sg (an empty group past the end)
+  auto issue = [&](int64_t st, int sg) {
+    if (st < nsub) {
+      const int64_t xb = sub_base(st);
+      E* sp = ring + (size_t)sg * 2 * R * 32 + lane;
+#pragma unroll
+      for (int r = 0; r < R; ++r) cp_async_amp(sp + r * 32, gp + (xb | hoff[r]));
+      if (load_lambda) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) cp_async_amp(sp + (R + r) * 32, gl + (xb | hoff[r]));
+      }
+    }
+    cp_async_commit();
+  };
+  FFAcc ax, ac, ae;
+  ax.zero();
+  ac.zero();
+  ae.zero();
+  const Coef rc = P.rx_c, rs = P.rx_s;
+  int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  __syncthreads();  // coefficient table staged
+#pragma unroll
+  for (int k = 0; k < ADJW_STAGES - 1; ++k) issue(st + k * wstride, k);
+  int sg = 0;
+  for (; st < nsub; st += wstride) {
+    cp_async_wait<ADJW_STAGES - 2>();  // this sub-tile's group has landed
+    const int64_t xb = sub_base(st);
+    E a[R], l[R];
+    {
+      const E* sp = ring + (size_t)sg * 2 * R * 32 + lane;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        a[r] = sp[r * 32];
+        if (load_lambda) l[r] = sp[(R + r) * 32];
+      }
+    }
+    // refill the stage read one iteration ago (its values are in registers)
+    issue(st + (ADJW_STAGES - 1) * wstride, sg == 0 ? ADJW_STAGES - 1 : sg - 1);
+    sg = sg + 1 == ADJW_STAGES ? 0 : sg + 1;
+
+    if (P.init) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float c = (float)P.cuts[xb | hoff[r]];
+        FFAcc t;
+        t.zero();
+        acc_norm2(t, a[r]);
+        ae.add_prod(c, 0.f, t.s, t.e);
+        l[r] = scale_ff(a[r], c);
+      }
+    }
+    // mixer: each bit's reduction precedes its own RX(-beta); the
+    // reduction on bit j is unchanged by RX already undone on other bits
+    // (same unitary on both vectors) and commutes with X_j
+    if (P.lanes) {
+      for (int b = 0; b < 5; ++b) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const E pa = shfl_xor_e(a[r], 1 << b);
+          const E pl = shfl_xor_e(l[r], 1 << b);
+          redx_acc(ax, l[r], pa);
+          a[r] = rx_one(rc, rs, a[r], pa);
+          l[r] = rx_one(rc, rs, l[r], pl);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < RB; ++j) {
+      if (j < P.nact) {
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+          const int i0 = ((i >> j) << (j + 1)) | (i & ((1 << j) - 1));
+          const int i1 = i0 | (1 << j);
+          redx_acc(ax, l[i0], a[i1]);
+          redx_acc(ax, l[i1], a[i0]);
+          const E a0 = a[i0], l0 = l[i0];
+          a[i0] = rx_one(rc, rs, a0, a[i1]);
+          a[i1] = rx_one(rc, rs, a[i1], a0);
+          l[i0] = rx_one(rc, rs, l0, l[i1]);
+          l[i1] = rx_one(rc, rs, l[i1], l0);
+        }
+      }
+    }
+    if (P.last) {
+      uint32_t cv[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) cv[r] = P.cuts[xb | hoff[r]];
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc_imconj(ac, to_ff(l[r]), to_ff(a[r]), P.wref - (float)cv[r]);
+      for (int d = 0; d < P.ndiag; ++d) {
+        const int gb = P.diag_bit[d];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const Coef& c = scoef[2 * d + (((xb | hoff[r]) >> gb) & 1)];
+          a[r] = cmulv(c, a[r]);
+          l[r] = cmulv(c, l[r]);
+        }
+      }
+      const Coef* tab = scoef + 2 * P.ndiag;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const Coef& c = tab[min((int)cv[r], P.ncut - 1)];
+        a[r] = cmulv(c, a[r]);
+        l[r] = cmulv(c, l[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      gp[xb | hoff[r]] = a[r];
+      gl[xb | hoff[r]] = l[r];
+    }
+  }
+  cp_async_wait<0>();
+  // per-CTA sums of the three accumulators into this CTA's row
+  const double v[3] = {warp_sum((double)ax.s + (double)ax.e), warp_sum((double)ac.s + (double)ac.e),
+                       warp_sum((double)ae.s + (double)ae.e)};
+  if (lane == 0)
+    for (int k = 0; k < 3; ++k) red[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int slot = threadIdx.x == 0 ? P.slot_x : (threadIdx.x == 1 ? P.slot_cut : P.slot_e);
+    if (slot >= 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+      const float sc = threadIdx.x == 1 ? -2.f : 1.f;
+      P.rows[(size_t)blockIdx.x * P.nslots + slot] += sc * t;
+    }
+  }
+}
+
+// out[s] = sum over rows of rows[r][s]; one warp per slot, fixed order
+__global__ void k_rows_sum(const double* rows, int nrows, int nslots, double* out) {
+  const int s = blockIdx.x;
+  if (s >= nslots) return;
+  double v = 0.0;
+  for (int r = threadIdx.x; r < nrows; r += 32) v += rows[(size_t)r * nslots + s];
+  v = warp_sum(v);
+  if (threadIdx.x == 0) out[s] = v;
 }
 
 void qaoa_layer_ops(int n, const uint16_t* cuts, int nedges, double beta, double gamma,
                     const double* node_theta, std::vector<HostOp>& ops);
+
+int g_adjoint_smem_only = 0;  // qf_set_tile_kernel(1): shared-memory adjoint kernel only
 
 int adj_grid(int n, int layout) {
   const int TB = layout == C64 ? 11 : 10;
@@ -337,10 +586,122 @@ int adj_grid(int n, int layout) {
   return (int)g;
 }
 
+extern int g_warp_rb_override;
+
+// register bits of k_adjw: 2 or 3 for FP64/float-float, 3 or 4 for complex64
+int adjw_rb(int layout) {
+  const int o = g_warp_rb_override;
+  if (layout == C64) return (o == 3 || o == 4) ? o : 3;
+  return (o == 2 || o == 3) ? o : 2;
+}
+
+int adjw_grid(int n, int layout) {
+  const int rb = adjw_rb(layout);
+  if (n < 5 + rb) return 0;
+  const int64_t nsub = int64_t(1) << (n - 5 - rb);
+  int64_t g = (nsub + 7) / 8;
+  const int64_t cap = (int64_t)device_sm_count() * 4;
+  return (int)(g < cap ? g : cap);
+}
+
 size_t qaoa_grad_workspace_bytes(int n, int p, int layout) {
   const size_t amps = size_t(1) << n;
   const int nslots = 2 * p + 1;
-  return amps * elem_bytes(layout) + (size_t)adj_grid(n, layout) * nslots * sizeof(double) + 256;
+  const int rows = std::max(adj_grid(n, layout), adjw_grid(n, layout));
+  return amps * elem_bytes(layout) + (size_t)rows * nslots * sizeof(double) + 512;
+}
+
+template <int LAY, int RB>
+static int launch_adjw(AdjWParams& P, int grid, cudaStream_t stream) {
+  static std::atomic<bool> attr[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr[dev].load()) {
+    int rc = check_cuda(cudaFuncSetAttribute(k_adjw<LAY, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(adjw_ring_bytes<LAY, RB>() + ADJW_MAX_COEF * sizeof(Coef) + 128)));
+    if (rc) return rc;
+    attr[dev].store(true);
+  }
+  const size_t necoef = (size_t)(2 * P.ndiag + P.ncut);
+  const size_t smem = ((necoef * sizeof(Coef) + 127) & ~size_t(127)) + adjw_ring_bytes<LAY, RB>();
+  k_adjw<LAY, RB><<<grid, 256, smem, stream>>>(P);
+  return check_cuda(cudaGetLastError());
+}
+
+// Warp-tile adjoint sweep (k_adjw); psi holds the forward state.  Per layer
+// the high bits 5..n-1 are taken RB at a time (the last group may act on
+// fewer, its register index padded with other high bits that are carried
+// unchanged); the first pass also undoes the mixer on the lane bits, the
+// last one the cost layer.
+static int qaoa_grad_warp(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
+                          const double* gamma, const double* node_theta, void* lam, double* rows, int nslots,
+                          cudaStream_t stream) {
+  const int RB = adjw_rb(layout);
+  const int grid = adjw_grid(n, layout);
+  static thread_local AdjWParams P;
+  std::vector<std::vector<int>> groups;
+  for (int b = 5; b < n; b += RB) {
+    std::vector<int> g;
+    for (int k = b; k < std::min(n, b + RB); ++k) g.push_back(k);
+    groups.push_back(g);
+  }
+  const double half_e = 0.5 * nedges;
+  std::memset(&P, 0, sizeof(P));
+  P.psi = psi;
+  P.lam = lam;
+  P.cuts = cuts;
+  P.rows = rows;
+  P.n = n;
+  P.nslots = nslots;
+  P.wref = (float)half_e;
+  int nd = 0;
+  if (node_theta != nullptr) {
+    for (int q = 0; q < n; ++q) {
+      if (std::isnan(node_theta[q])) continue;
+      P.diag_bit[nd] = (uint8_t)(n - 1 - q);
+      P.coef[2 * nd] = make_coef(std::polar(1.0, 0.5 * node_theta[q]), layout);
+      P.coef[2 * nd + 1] = make_coef(std::polar(1.0, -0.5 * node_theta[q]), layout);
+      ++nd;
+    }
+  }
+  P.ndiag = nd;
+  P.ncut = nedges + 1;
+  if (2 * nd + P.ncut > ADJW_MAX_COEF) return QF_ERR_TOO_LARGE;
+  bool first = true;
+  for (int l = p - 1; l >= 0; --l) {
+    P.rx_c = make_coef(cplx(std::cos(0.5 * beta[l]), 0.0), layout);
+    P.rx_s = make_coef(cplx(std::sin(0.5 * beta[l]), 0.0), layout);
+    for (int cv = 0; cv <= nedges; ++cv)
+      P.coef[2 * nd + cv] = make_coef(std::polar(1.0, -gamma[l] * (half_e - cv)), layout);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      std::vector<int> hb = groups[gi];
+      for (int b = 5; b < n && (int)hb.size() < RB; ++b)
+        if (std::find(hb.begin(), hb.end(), b) == hb.end()) hb.push_back(b);
+      for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];  // acted-on bits first
+      std::sort(hb.begin(), hb.end());
+      for (int j = 0; j < RB; ++j) P.hs[j] = (uint8_t)hb[j];
+      P.init = first ? 1 : 0;
+      P.lanes = gi == 0 ? 1 : 0;
+      P.nact = (int)groups[gi].size();
+      P.last = gi + 1 == groups.size() ? 1 : 0;
+      P.slot_x = p + l;
+      P.slot_cut = P.last ? l : -1;
+      P.slot_e = first ? 2 * p : -1;
+      int rc;
+      switch (layout * 8 + RB) {
+        case C64 * 8 + 3: rc = launch_adjw<C64, 3>(P, grid, stream); break;
+        case C64 * 8 + 4: rc = launch_adjw<C64, 4>(P, grid, stream); break;
+        case C128 * 8 + 2: rc = launch_adjw<C128, 2>(P, grid, stream); break;
+        case C128 * 8 + 3: rc = launch_adjw<C128, 3>(P, grid, stream); break;
+        case FF * 8 + 2: rc = launch_adjw<FF, 2>(P, grid, stream); break;
+        case FF * 8 + 3: rc = launch_adjw<FF, 3>(P, grid, stream); break;
+        default: rc = QF_ERR_LAYOUT;
+      }
+      if (rc) return rc;
+      first = false;
+    }
+  }
+  return QF_OK;
 }
 
 template <int LAY>
@@ -371,6 +732,16 @@ int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, in
   double* rows = reinterpret_cast<double*>(reinterpret_cast<char*>(ws) + ((amps * elem_bytes(layout) + 255) & ~size_t(255)));
   const int nslots = 2 * p + 1;
   if (nslots > ADJ_MAX_SLOTS) return QF_ERR_TOO_LARGE;
+  const int wgrid = adjw_grid(n, layout);
+  const bool wfits = 4 + 2 * n + nedges + 1 <= ADJW_MAX_COEF;  // coefficient table of one pass
+  if (wgrid > 0 && p > 0 && wfits && !g_adjoint_smem_only) {
+    int rc = check_cuda(cudaMemsetAsync(rows, 0, (size_t)wgrid * nslots * sizeof(double), stream));
+    if (rc) return rc;
+    rc = qaoa_grad_warp(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, lam, rows, nslots, stream);
+    if (rc) return rc;
+    k_rows_sum<<<nslots, 32, 0, stream>>>(rows, wgrid, nslots, out);
+    return check_cuda(cudaGetLastError());
+  }
   const int grid = adj_grid(n, layout);
   int rc = check_cuda(cudaMemsetAsync(rows, 0, (size_t)grid * nslots * sizeof(double), stream));
   if (rc) return rc;
@@ -504,7 +875,7 @@ int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, in
   if (p == 0) {  // <C> only
     return reduce_diag(psi, n, layout, 1, cuts, nullptr, out + 2 * p, rows, stream);
   }
-  k_rows_sum<<<1, 64, 0, stream>>>(rows, grid, nslots, out);
+  k_rows_sum<<<nslots, 32, 0, stream>>>(rows, grid, nslots, out);
   return check_cuda(cudaGetLastError());
 }
 

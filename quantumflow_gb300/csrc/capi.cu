@@ -11,6 +11,7 @@
 namespace qf {
 extern thread_local int t_last_cuda_error;
 extern int g_force_smem_tile;
+extern int g_adjoint_smem_only;
 extern int g_warp_rb_override;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
@@ -91,6 +92,7 @@ int qf_get_device_error(int* flags, void* stream) {
 int qf_set_tile_kernel(int mode) {
   if (mode < 0 || mode > 4) return QF_ERR_INVALID_ARGUMENT;
   g_force_smem_tile = mode == 1;
+  g_adjoint_smem_only = mode == 1;
   g_warp_rb_override = mode >= 2 ? mode : 0;
   return QF_OK;
 }

@@ -515,6 +515,16 @@ QF_D void g2_reg_dispatch(int j0, int j1, const Coef* cf, E (&a)[1 << RB]) {
 
 template <int RB, typename E>
 QF_D void g1_lane(int l, const Coef* cf, E (&a)[1 << RB], int lane) {
+  if (coef_symmetric(cf)) {
+    // both lanes compute c0 self + c1 partner with uniform coefficients
+    // (zero parts skipped: RX costs half a dense row)
+#pragma unroll
+    for (int r = 0; r < (1 << RB); ++r) {
+      const E p[2] = {a[r], shfl_xor(a[r], 1 << l)};
+      a[r] = cdot<2>(cf, p);
+    }
+    return;
+  }
   const int hi = (lane >> l) & 1;
   E* tag = nullptr;
   const E cs = coef_e(cf[hi * 3], tag);

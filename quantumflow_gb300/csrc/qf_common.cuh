@@ -296,6 +296,29 @@ QF_D void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::
 QF_D void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 QF_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Per-thread asynchronous global -> shared copies of one amplitude (8 or 16
+// bytes), tracked in the issuing thread's cp.async groups.  A thread that
+// reads back only what it copied itself needs no barrier, only wait_group.
+QF_D void cp_async_amp(float4* s, const float4* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(s)), "l"(g) : "memory");
+}
+QF_D void cp_async_amp(double2* s, const double2* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(s)), "l"(g) : "memory");
+}
+QF_D void cp_async_amp(float2* s, const float2* g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(s)), "l"(g) : "memory");
+}
+QF_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+QF_D void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Uniform test: the 2x2 matrix cf[0..3] has equal diagonal and equal
+// off-diagonal entries (RX, H-free mixers): both rows read c0 self + c1 partner.
+QF_D bool coef_symmetric(const Coef* cf) {
+  return cf[0].d[0] == cf[3].d[0] && cf[0].d[1] == cf[3].d[1] && cf[1].d[0] == cf[2].d[0] &&
+         cf[1].d[1] == cf[2].d[1];
+}
+
 // ---------------------------------------------------- warp reductions ----
 QF_D double warp_sum(double v) {
 #pragma unroll

@@ -193,3 +193,47 @@ def test_circuit_expectation_autograd():
     e.backward()
     _, grads = qf.adjoint.expectation_and_grad(_param_circuit(theta.detach().numpy()), diag)
     np.testing.assert_allclose(theta.grad.numpy(), [grads[k] for k in keys], atol=1e-12)
+
+
+@pytest.mark.parametrize("arith", ["ff", "fp64", "c64"])
+@pytest.mark.parametrize("n", [7, 8, 9, 12, 15])
+def test_warp_adjoint_equals_shared_memory_adjoint(n, arith, monkeypatch):
+    """The warp-tile adjoint (default for n >= 5 + register bits), with each
+    register-bit count it offers, agrees with the shared-memory adjoint
+    kernel on graphs with node weights; both leave psi at |+>^n.  Covers
+    the float-float, native FP64 and complex64 layouts."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    from quantumflow_gb300 import qaoa as qaoa_mod
+    dtype = "complex64" if arith == "c64" else "complex128"
+    if arith == "fp64":
+        monkeypatch.setattr(qaoa_mod, "compute_layout", lambda d: nat.LAYOUT_C128)
+    elif arith == "ff":
+        monkeypatch.setattr(qaoa_mod, "compute_layout", lambda d: nat.LAYOUT_FF)
+    p = 3
+    g = qf.qaoa.gnp_random_graph(n, 0.45, seed=n)
+    g.nodes[1]["weight"] = 0.4
+    g.nodes[n - 2]["weight"] = -0.9
+    rng = np.random.default_rng(n)
+    beta, gamma = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
+    results = {}
+    modes = (1, 0, 2, 3) if dtype == "complex128" else (1, 0, 3, 4)
+    try:
+        for mode in modes:
+            nat.call("qf_set_tile_kernel", mode)
+            prob = qf.QAOAMaxCut(g, p, dtype=dtype)
+            e, gb, gg = prob.expectation_and_grad(beta, gamma)
+            results[mode] = np.concatenate([[e], gb, gg])
+            plus = qf.State(prob._grad_bufs[1]).asarray().reshape(-1)
+            assert np.max(np.abs(plus - 2 ** (-n / 2))) < (1e-12 if dtype == "complex128" else 1e-5)
+    finally:
+        nat.call("qf_set_tile_kernel", 0)
+    tol = 1e-10 if dtype == "complex128" else 2e-4
+    for mode in modes[1:]:
+        np.testing.assert_allclose(results[mode], results[1], atol=tol * max(1.0, np.max(np.abs(results[1]))))
+    if dtype == "complex128":
+        nw = [g.nodes[q].get("weight", None) for q in range(n)]
+        fg, fb = orc.qaoa_fd_gradient(n, g.edges(), p, beta, gamma, 1e-6, None, nw) if n <= 9 else (None, None)
+        if fg is not None:
+            np.testing.assert_allclose(results[0][1:1 + p], fb, atol=2e-7)
+            np.testing.assert_allclose(results[0][1 + p:], fg, atol=2e-7)
