@@ -64,76 +64,6 @@ struct AdjParams {
   Coef coef[ADJ_MAX_COEF];
 };
 
-QF_D float2 cmulv(const Coef& c, float2 a) {
-  const float ur = c.f[0], ui = c.f[2];
-  return make_float2(fmaf(ur, a.x, -ui * a.y), fmaf(ur, a.y, ui * a.x));
-}
-QF_D double2 cmulv(const Coef& c, double2 a) {
-  const double ur = c.d[0], ui = c.d[1];
-  return make_double2(fma(ur, a.x, -ui * a.y), fma(ur, a.y, ui * a.x));
-}
-QF_D float4 cmulv(const Coef& c, float4 a) {
-  FFAcc re, im;
-  re.zero();
-  im.zero();
-  re.add_prod(c.f[0], c.f[1], a.x, a.y);
-  re.add_prod(-c.f[2], -c.f[3], a.z, a.w);
-  im.add_prod(c.f[0], c.f[1], a.z, a.w);
-  im.add_prod(c.f[2], c.f[3], a.x, a.y);
-  float4 r;
-  re.finish(r.x, r.y);
-  im.finish(r.z, r.w);
-  return r;
-}
-QF_D float4 scale_ff(float4 a, float c) {  // exact-product scaling by a small integer-valued float
-  float4 r;
-  FFAcc t;
-  t.zero();
-  t.add_prod(c, 0.f, a.x, a.y);
-  t.finish(r.x, r.y);
-  t.zero();
-  t.add_prod(c, 0.f, a.z, a.w);
-  t.finish(r.z, r.w);
-  return r;
-}
-QF_D float2 scale_ff(float2 a, float c) { return make_float2(a.x * c, a.y * c); }
-QF_D double2 scale_ff(double2 a, float c) { return make_double2(a.x * (double)c, a.y * (double)c); }
-
-// acc += w * Im(conj(l) * p), with Im(conj(l) p) formed in float-float
-// first and then multiplied by w exactly (w is a small half-integer).
-QF_D void acc_imconj(FFAcc& acc, float4 l, float4 p, float w) {
-  FFAcc t;
-  t.zero();
-  t.add_prod(l.x, l.y, p.z, p.w);
-  t.add_prod(-l.z, -l.w, p.x, p.y);
-  if (w == 1.f) {
-    acc.add(t.s, t.e);
-  } else {
-    acc.add_prod(w, 0.f, t.s, t.e);
-  }
-}
-QF_D void acc_imconj(FFAcc& acc, float2 l, float2 p, float w) {
-  FFAcc t;
-  t.zero();
-  t.add_prod(l.x, 0.f, p.y, 0.f);
-  t.add_prod(-l.y, 0.f, p.x, 0.f);
-  acc.add_prod(w, 0.f, t.s, t.e);
-}
-QF_D void acc_imconj(FFAcc& acc, double2 l, double2 p, float w) {
-  acc_imconj(acc, to_ff(l), to_ff(p), w);
-}
-
-
-QF_D float2 shfl_xor_e(float2 v, int m) {
-  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-QF_D double2 shfl_xor_e(double2 v, int m) {
-  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-QF_D float4 shfl_xor_e(float4 v, int m) {
-  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
-                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
-}
 QF_D int64_t adj_global(const AdjParams& P, int64_t base, int l) {
   int64_t x = base | (l & ((1 << P.L) - 1));
   for (int r = 0; r < P.nh; ++r)
@@ -290,8 +220,8 @@ __global__ void __launch_bounds__(256) k_adj(const __grid_constant__ AdjParams P
           for (int l = tid; l < T; l += nthr) {
             const int64_t x = adj_global(P, base, l);
             const int c = min((int)P.cuts[x], op.ncoef - 1);
-            sp[l] = cmulv(cf[c], sp[l]);
-            sl[l] = cmulv(cf[c], sl[l]);
+            sp[l] = cmul_v(cf[c], sp[l]);
+            sl[l] = cmul_v(cf[c], sl[l]);
           }
           break;
         }
@@ -299,8 +229,8 @@ __global__ void __launch_bounds__(256) k_adj(const __grid_constant__ AdjParams P
           for (int l = tid; l < T; l += nthr) {
             const int64_t x = adj_global(P, base, l);
             const Coef& c = cf[(x >> op.gb) & 1];
-            sp[l] = cmulv(c, sp[l]);
-            sl[l] = cmulv(c, sl[l]);
+            sp[l] = cmul_v(c, sp[l]);
+            sl[l] = cmul_v(c, sl[l]);
           }
           break;
         }
@@ -351,48 +281,16 @@ struct AdjWParams {
   int32_t nact;   // ... and on register bits 0..nact-1
   int32_t last;   // cut reduction, node phases (ndiag), cut phase (ncut entries)
   int32_t ndiag, ncut;
-  int32_t slot_x, slot_cut, slot_e;  // output slots of the three accumulators (-1: unused)
+  int32_t hasB, nactB;               // stage B: the previous layer's mixer on lanes + bits 0..nactB-1
+  int32_t slot_x, slot_cut, slot_e, slot_xb;  // output slots of the four accumulators (-1: unused)
   float wref;                        // E/2
   uint8_t hb[4];                     // global bit of each register index bit
   uint8_t hs[4];                     // the same bits in ascending order
   uint8_t diag_bit[QF_MAX_QUBITS];   // global bit of each node phase
   Coef rx_c, rx_s;                   // RX(-beta) = [[c, i s], [i s, c]]
+  Coef b_c, b_s;                     // the same for stage B's layer
   Coef coef[ADJW_MAX_COEF];          // node phase pairs, then the cut table
 };
-
-// float-float a*x + b*y: both products exact to 2^-48, one TwoSum, one
-// renormalisation
-QF_D void ff_dot2(float ah, float al, float xh, float xl, float bh, float bl, float yh, float yl, float& rh,
-                  float& rl) {
-  float p0, c0, p1, c1, s, t;
-  ff_term(ah, al, xh, xl, p0, c0);
-  ff_term(bh, bl, yh, yl, p1, c1);
-  two_sum(p0, p1, s, t);
-  fast_two_sum(s, __fadd_rn(__fadd_rn(c0, c1), t), rh, rl);
-}
-// c a + i s p for real c, s (RX(-beta) row applied to self a and partner p)
-QF_D float4 rx_one(const Coef& c, const Coef& s, float4 a, float4 p) {
-  float4 o;
-  ff_dot2(c.f[0], c.f[1], a.x, a.y, -s.f[0], -s.f[1], p.z, p.w, o.x, o.y);
-  ff_dot2(c.f[0], c.f[1], a.z, a.w, s.f[0], s.f[1], p.x, p.y, o.z, o.w);
-  return o;
-}
-QF_D double2 rx_one(const Coef& c, const Coef& s, double2 a, double2 p) {
-  return make_double2(fma(c.d[0], a.x, -s.d[0] * p.y), fma(c.d[0], a.y, s.d[0] * p.x));
-}
-QF_D float2 rx_one(const Coef& c, const Coef& s, float2 a, float2 p) {
-  return make_float2(fmaf(c.f[0], a.x, -s.f[0] * p.y), fmaf(c.f[0], a.y, s.f[0] * p.x));
-}
-// acc += Im(conj(l) p)
-QF_D void redx_acc(FFAcc& acc, float4 l, float4 p) {
-  acc.add_prod(l.x, l.y, p.z, p.w);
-  acc.add_prod(-l.z, -l.w, p.x, p.y);
-}
-QF_D void redx_acc(FFAcc& acc, double2 l, double2 p) { acc_imconj(acc, l, p, 1.f); }
-QF_D void redx_acc(FFAcc& acc, float2 l, float2 p) {
-  acc.add_prod(l.x, 0.f, p.y, 0.f);
-  acc.add_prod(-l.y, 0.f, p.x, 0.f);
-}
 
 template <int LAY, int RB>
 constexpr size_t adjw_ring_bytes() {
@@ -405,7 +303,7 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
   constexpr int R = 1 << RB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Coef* scoef = reinterpret_cast<Coef*>(smem_raw);
-  __shared__ double red[8][3];
+  __shared__ double red[8][4];
   const int necoef = 2 * P.ndiag + P.ncut;
   for (int i = threadIdx.x; i < necoef; i += blockDim.x) scoef[i] = P.coef[i];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -446,10 +344,11 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
     }
     cp_async_commit();
   };
-  FFAcc ax, ac, ae;
+  FFAcc ax, ac, ae, axb;
   ax.zero();
   ac.zero();
   ae.zero();
+  axb.zero();
   const Coef rc = P.rx_c, rs = P.rx_s;
   int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
   __syncthreads();  // coefficient table staged
@@ -486,35 +385,38 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
     // mixer: each bit's reduction precedes its own RX(-beta); the
     // reduction on bit j is unchanged by RX already undone on other bits
     // (same unitary on both vectors) and commutes with X_j
-    if (P.lanes) {
-      for (int b = 0; b < 5; ++b) {
+    auto mixer = [&](const Coef& mc, const Coef& ms, bool lanes, int nact, FFAcc& acc) {
+      if (lanes) {
+        for (int b = 0; b < 5; ++b) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const E pa = shfl_xor_e(a[r], 1 << b);
-          const E pl = shfl_xor_e(l[r], 1 << b);
-          redx_acc(ax, l[r], pa);
-          a[r] = rx_one(rc, rs, a[r], pa);
-          l[r] = rx_one(rc, rs, l[r], pl);
+          for (int r = 0; r < R; ++r) {
+            const E pa = shfl_xor(a[r], 1 << b);
+            const E pl = shfl_xor(l[r], 1 << b);
+            redx_acc(acc, l[r], pa);
+            a[r] = rx_one(mc, ms, a[r], pa);
+            l[r] = rx_one(mc, ms, l[r], pl);
+          }
         }
       }
-    }
 #pragma unroll
-    for (int j = 0; j < RB; ++j) {
-      if (j < P.nact) {
+      for (int j = 0; j < RB; ++j) {
+        if (j < nact) {
 #pragma unroll
-        for (int i = 0; i < R / 2; ++i) {
-          const int i0 = ((i >> j) << (j + 1)) | (i & ((1 << j) - 1));
-          const int i1 = i0 | (1 << j);
-          redx_acc(ax, l[i0], a[i1]);
-          redx_acc(ax, l[i1], a[i0]);
-          const E a0 = a[i0], l0 = l[i0];
-          a[i0] = rx_one(rc, rs, a0, a[i1]);
-          a[i1] = rx_one(rc, rs, a[i1], a0);
-          l[i0] = rx_one(rc, rs, l0, l[i1]);
-          l[i1] = rx_one(rc, rs, l[i1], l0);
+          for (int i = 0; i < R / 2; ++i) {
+            const int i0 = ((i >> j) << (j + 1)) | (i & ((1 << j) - 1));
+            const int i1 = i0 | (1 << j);
+            redx_acc(acc, l[i0], a[i1]);
+            redx_acc(acc, l[i1], a[i0]);
+            const E a0 = a[i0], l0 = l[i0];
+            a[i0] = rx_one(mc, ms, a0, a[i1]);
+            a[i1] = rx_one(mc, ms, a[i1], a0);
+            l[i0] = rx_one(mc, ms, l0, l[i1]);
+            l[i1] = rx_one(mc, ms, l[i1], l0);
+          }
         }
       }
-    }
+    };
+    mixer(rc, rs, P.lanes != 0, P.nact, ax);
     if (P.last) {
       uint32_t cv[R];
 #pragma unroll
@@ -526,18 +428,19 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const Coef& c = scoef[2 * d + (((xb | hoff[r]) >> gb) & 1)];
-          a[r] = cmulv(c, a[r]);
-          l[r] = cmulv(c, l[r]);
+          a[r] = cmul_v(c, a[r]);
+          l[r] = cmul_v(c, l[r]);
         }
       }
       const Coef* tab = scoef + 2 * P.ndiag;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const Coef& c = tab[min((int)cv[r], P.ncut - 1)];
-        a[r] = cmulv(c, a[r]);
-        l[r] = cmulv(c, l[r]);
+        a[r] = cmul_v(c, a[r]);
+        l[r] = cmul_v(c, l[r]);
       }
     }
+    if (P.hasB) mixer(P.b_c, P.b_s, true, P.nactB, axb);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       gp[xb | hoff[r]] = a[r];
@@ -545,14 +448,15 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
     }
   }
   cp_async_wait<0>();
-  // per-CTA sums of the three accumulators into this CTA's row
-  const double v[3] = {warp_sum((double)ax.s + (double)ax.e), warp_sum((double)ac.s + (double)ac.e),
-                       warp_sum((double)ae.s + (double)ae.e)};
+  // per-CTA sums of the four accumulators into this CTA's row
+  const double v[4] = {warp_sum((double)ax.s + (double)ax.e), warp_sum((double)ac.s + (double)ac.e),
+                       warp_sum((double)ae.s + (double)ae.e), warp_sum((double)axb.s + (double)axb.e)};
   if (lane == 0)
-    for (int k = 0; k < 3; ++k) red[warp][k] = v[k];
+    for (int k = 0; k < 4; ++k) red[warp][k] = v[k];
   __syncthreads();
-  if (threadIdx.x < 3) {
-    const int slot = threadIdx.x == 0 ? P.slot_x : (threadIdx.x == 1 ? P.slot_cut : P.slot_e);
+  if (threadIdx.x < 4) {
+    const int k = threadIdx.x;
+    const int slot = k == 0 ? P.slot_x : k == 1 ? P.slot_cut : k == 2 ? P.slot_e : P.slot_xb;
     if (slot >= 0) {
       double t = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
@@ -667,39 +571,61 @@ static int qaoa_grad_warp(void* psi, int n, int layout, const uint16_t* cuts, in
   P.ndiag = nd;
   P.ncut = nedges + 1;
   if (2 * nd + P.ncut > ADJW_MAX_COEF) return QF_ERR_TOO_LARGE;
+  const int m = (int)groups.size();
+  // layer l (counted from the last) visits the groups forwards or backwards
+  // so that its last group is the next layer's first: that pass also runs
+  // the next layer's mixer on the lanes and the same group (stage B)
+  auto order = [&](int l, int k) { return ((p - 1 - l) & 1) ? m - 1 - k : k; };
+  auto set_group = [&](int gi) {
+    std::vector<int> hb = groups[gi];
+    for (int b = 5; b < n && (int)hb.size() < RB; ++b)
+      if (std::find(hb.begin(), hb.end(), b) == hb.end()) hb.push_back(b);
+    for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];  // acted-on bits first
+    std::sort(hb.begin(), hb.end());
+    for (int j = 0; j < RB; ++j) P.hs[j] = (uint8_t)hb[j];
+    return (int)groups[gi].size();
+  };
+  auto launch = [&]() {
+    switch (layout * 8 + RB) {
+      case C64 * 8 + 3: return launch_adjw<C64, 3>(P, grid, stream);
+      case C64 * 8 + 4: return launch_adjw<C64, 4>(P, grid, stream);
+      case C128 * 8 + 2: return launch_adjw<C128, 2>(P, grid, stream);
+      case C128 * 8 + 3: return launch_adjw<C128, 3>(P, grid, stream);
+      case FF * 8 + 2: return launch_adjw<FF, 2>(P, grid, stream);
+      case FF * 8 + 3: return launch_adjw<FF, 3>(P, grid, stream);
+    }
+    return (int)QF_ERR_LAYOUT;
+  };
   bool first = true;
+  bool lanes_done = false;  // the layer's lane bits were undone by the previous pass's stage B
   for (int l = p - 1; l >= 0; --l) {
     P.rx_c = make_coef(cplx(std::cos(0.5 * beta[l]), 0.0), layout);
     P.rx_s = make_coef(cplx(std::sin(0.5 * beta[l]), 0.0), layout);
     for (int cv = 0; cv <= nedges; ++cv)
       P.coef[2 * nd + cv] = make_coef(std::polar(1.0, -gamma[l] * (half_e - cv)), layout);
-    for (size_t gi = 0; gi < groups.size(); ++gi) {
-      std::vector<int> hb = groups[gi];
-      for (int b = 5; b < n && (int)hb.size() < RB; ++b)
-        if (std::find(hb.begin(), hb.end(), b) == hb.end()) hb.push_back(b);
-      for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];  // acted-on bits first
-      std::sort(hb.begin(), hb.end());
-      for (int j = 0; j < RB; ++j) P.hs[j] = (uint8_t)hb[j];
+    for (int k = lanes_done ? 1 : 0; k < m; ++k) {
+      const int nact = set_group(order(l, k));
       P.init = first ? 1 : 0;
-      P.lanes = gi == 0 ? 1 : 0;
-      P.nact = (int)groups[gi].size();
-      P.last = gi + 1 == groups.size() ? 1 : 0;
+      P.lanes = k == 0 ? 1 : 0;
+      P.nact = nact;
+      P.last = k == m - 1 ? 1 : 0;
       P.slot_x = p + l;
       P.slot_cut = P.last ? l : -1;
       P.slot_e = first ? 2 * p : -1;
-      int rc;
-      switch (layout * 8 + RB) {
-        case C64 * 8 + 3: rc = launch_adjw<C64, 3>(P, grid, stream); break;
-        case C64 * 8 + 4: rc = launch_adjw<C64, 4>(P, grid, stream); break;
-        case C128 * 8 + 2: rc = launch_adjw<C128, 2>(P, grid, stream); break;
-        case C128 * 8 + 3: rc = launch_adjw<C128, 3>(P, grid, stream); break;
-        case FF * 8 + 2: rc = launch_adjw<FF, 2>(P, grid, stream); break;
-        case FF * 8 + 3: rc = launch_adjw<FF, 3>(P, grid, stream); break;
-        default: rc = QF_ERR_LAYOUT;
+      P.hasB = 0;
+      P.slot_xb = -1;
+      if (P.last && l > 0 && m > 1) {  // order(l-1, 0) == order(l, m-1)
+        P.hasB = 1;
+        P.nactB = nact;
+        P.b_c = make_coef(cplx(std::cos(0.5 * beta[l - 1]), 0.0), layout);
+        P.b_s = make_coef(cplx(std::sin(0.5 * beta[l - 1]), 0.0), layout);
+        P.slot_xb = p + l - 1;
       }
+      const int rc = launch();
       if (rc) return rc;
       first = false;
     }
+    lanes_done = m > 1;
   }
   return QF_OK;
 }

@@ -66,44 +66,6 @@ int device_sm_count() {
   return v;
 }
 
-// ------------------------------------------------ per-thread coefficients --
-QF_D float2 coef_e(const Coef& c, float2*) { return make_float2(c.f[0], c.f[2]); }
-QF_D double2 coef_e(const Coef& c, double2*) { return make_double2(c.d[0], c.d[1]); }
-QF_D float4 coef_e(const Coef& c, float4*) { return make_float4(c.f[0], c.f[1], c.f[2], c.f[3]); }
-
-QF_D float2 cmul_v(const Coef& c, float2 a) {
-  const float ur = c.f[0], ui = c.f[2];
-  return make_float2(fmaf(ur, a.x, -ui * a.y), fmaf(ur, a.y, ui * a.x));
-}
-QF_D double2 cmul_v(const Coef& c, double2 a) {
-  const double ur = c.d[0], ui = c.d[1];
-  return make_double2(fma(ur, a.x, -ui * a.y), fma(ur, a.y, ui * a.x));
-}
-QF_D float4 cmul_v(const Coef& c, float4 a) {
-  FFAcc re, im;
-  re.zero();
-  im.zero();
-  re.add_prod(c.f[0], c.f[1], a.x, a.y);
-  re.add_prod(-c.f[2], -c.f[3], a.z, a.w);
-  im.add_prod(c.f[0], c.f[1], a.z, a.w);
-  im.add_prod(c.f[2], c.f[3], a.x, a.y);
-  float4 r;
-  re.finish(r.x, r.y);
-  im.finish(r.z, r.w);
-  return r;
-}
-
-QF_D float2 shfl_xor(float2 v, int m) {
-  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-QF_D double2 shfl_xor(double2 v, int m) {
-  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
-QF_D float4 shfl_xor(float4 v, int m) {
-  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
-                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
-}
-
 QF_D int ins0(int v, int b) { return ((v >> b) << (b + 1)) | (v & ((1 << b) - 1)); }
 
 struct CoefArr4 {
@@ -515,16 +477,6 @@ QF_D void g2_reg_dispatch(int j0, int j1, const Coef* cf, E (&a)[1 << RB]) {
 
 template <int RB, typename E>
 QF_D void g1_lane(int l, const Coef* cf, E (&a)[1 << RB], int lane) {
-  if (coef_symmetric(cf)) {
-    // both lanes compute c0 self + c1 partner with uniform coefficients
-    // (zero parts skipped: RX costs half a dense row)
-#pragma unroll
-    for (int r = 0; r < (1 << RB); ++r) {
-      const E p[2] = {a[r], shfl_xor(a[r], 1 << l)};
-      a[r] = cdot<2>(cf, p);
-    }
-    return;
-  }
   const int hi = (lane >> l) & 1;
   E* tag = nullptr;
   const E cs = coef_e(cf[hi * 3], tag);

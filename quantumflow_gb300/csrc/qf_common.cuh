@@ -147,6 +147,17 @@ QF_D float4 ff_cmac2(float4 u0, float4 a0, float4 u1, float4 a1) {
   return r;
 }
 
+// float-float a*x + b*y: both products exact to 2^-48, one TwoSum, one
+// renormalisation
+QF_D void ff_dot2(float ah, float al, float xh, float xl, float bh, float bl, float yh, float yl, float& rh,
+                  float& rl) {
+  float p0, c0, p1, c1, s, t;
+  ff_term(ah, al, xh, xl, p0, c0);
+  ff_term(bh, bl, yh, yl, p1, c1);
+  two_sum(p0, p1, s, t);
+  fast_two_sum(s, __fadd_rn(__fadd_rn(c0, c1), t), rh, rl);
+}
+
 template <int J>
 QF_D float4 cdot(const Coef* u, const float4* a) {
   if constexpr (J == 2) {
@@ -250,6 +261,102 @@ QF_HD int64_t insert0(int64_t v, int b) {
   return ((v >> b) << (b + 1)) | lo;
 }
 
+
+// ------------------------------------ per-amplitude helpers (all layouts) --
+QF_D float2 coef_e(const Coef& c, float2*) { return make_float2(c.f[0], c.f[2]); }
+QF_D double2 coef_e(const Coef& c, double2*) { return make_double2(c.d[0], c.d[1]); }
+QF_D float4 coef_e(const Coef& c, float4*) { return make_float4(c.f[0], c.f[1], c.f[2], c.f[3]); }
+
+QF_D float2 cmul_v(const Coef& c, float2 a) {
+  const float ur = c.f[0], ui = c.f[2];
+  return make_float2(fmaf(ur, a.x, -ui * a.y), fmaf(ur, a.y, ui * a.x));
+}
+QF_D double2 cmul_v(const Coef& c, double2 a) {
+  const double ur = c.d[0], ui = c.d[1];
+  return make_double2(fma(ur, a.x, -ui * a.y), fma(ur, a.y, ui * a.x));
+}
+QF_D float4 cmul_v(const Coef& c, float4 a) {
+  float4 r;
+  ff_dot2(c.f[0], c.f[1], a.x, a.y, -c.f[2], -c.f[3], a.z, a.w, r.x, r.y);
+  ff_dot2(c.f[0], c.f[1], a.z, a.w, c.f[2], c.f[3], a.x, a.y, r.z, r.w);
+  return r;
+}
+
+QF_D float2 shfl_xor(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+QF_D double2 shfl_xor(double2 v, int m) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+QF_D float4 shfl_xor(float4 v, int m) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                     __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
+}
+
+QF_D float4 scale_ff(float4 a, float c) {  // exact-product scaling by a small integer-valued float
+  float4 r;
+  FFAcc t;
+  t.zero();
+  t.add_prod(c, 0.f, a.x, a.y);
+  t.finish(r.x, r.y);
+  t.zero();
+  t.add_prod(c, 0.f, a.z, a.w);
+  t.finish(r.z, r.w);
+  return r;
+}
+QF_D float2 scale_ff(float2 a, float c) { return make_float2(a.x * c, a.y * c); }
+QF_D double2 scale_ff(double2 a, float c) { return make_double2(a.x * (double)c, a.y * (double)c); }
+
+// acc += w * Im(conj(l) * p), with Im(conj(l) p) formed in float-float
+// first and then multiplied by w exactly (w is a small half-integer).
+QF_D void acc_imconj(FFAcc& acc, float4 l, float4 p, float w) {
+  FFAcc t;
+  t.zero();
+  t.add_prod(l.x, l.y, p.z, p.w);
+  t.add_prod(-l.z, -l.w, p.x, p.y);
+  if (w == 1.f) {
+    acc.add(t.s, t.e);
+  } else {
+    acc.add_prod(w, 0.f, t.s, t.e);
+  }
+}
+QF_D void acc_imconj(FFAcc& acc, float2 l, float2 p, float w) {
+  FFAcc t;
+  t.zero();
+  t.add_prod(l.x, 0.f, p.y, 0.f);
+  t.add_prod(-l.y, 0.f, p.x, 0.f);
+  acc.add_prod(w, 0.f, t.s, t.e);
+}
+QF_D void acc_imconj(FFAcc& acc, double2 l, double2 p, float w) {
+  acc_imconj(acc, to_ff(l), to_ff(p), w);
+}
+
+
+// c a + i s p for real c, s (RX(-beta) row applied to self a and partner p)
+QF_D float4 rx_one(const Coef& c, const Coef& s, float4 a, float4 p) {
+  float4 o;
+  ff_dot2(c.f[0], c.f[1], a.x, a.y, -s.f[0], -s.f[1], p.z, p.w, o.x, o.y);
+  ff_dot2(c.f[0], c.f[1], a.z, a.w, s.f[0], s.f[1], p.x, p.y, o.z, o.w);
+  return o;
+}
+QF_D double2 rx_one(const Coef& c, const Coef& s, double2 a, double2 p) {
+  return make_double2(fma(c.d[0], a.x, -s.d[0] * p.y), fma(c.d[0], a.y, s.d[0] * p.x));
+}
+QF_D float2 rx_one(const Coef& c, const Coef& s, float2 a, float2 p) {
+  return make_float2(fmaf(c.f[0], a.x, -s.f[0] * p.y), fmaf(c.f[0], a.y, s.f[0] * p.x));
+}
+// acc += Im(conj(l) p)
+QF_D void redx_acc(FFAcc& acc, float4 l, float4 p) {
+  acc.add_prod(l.x, l.y, p.z, p.w);
+  acc.add_prod(-l.z, -l.w, p.x, p.y);
+}
+QF_D void redx_acc(FFAcc& acc, double2 l, double2 p) { acc_imconj(acc, l, p, 1.f); }
+QF_D void redx_acc(FFAcc& acc, float2 l, float2 p) {
+  acc.add_prod(l.x, 0.f, p.y, 0.f);
+  acc.add_prod(-l.y, 0.f, p.x, 0.f);
+}
+
+
 // ---------------------------------------- mbarrier + bulk async copies -----
 QF_D uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -312,12 +419,6 @@ QF_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"
 template <int N>
 QF_D void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Uniform test: the 2x2 matrix cf[0..3] has equal diagonal and equal
-// off-diagonal entries (RX, H-free mixers): both rows read c0 self + c1 partner.
-QF_D bool coef_symmetric(const Coef* cf) {
-  return cf[0].d[0] == cf[3].d[0] && cf[0].d[1] == cf[3].d[1] && cf[1].d[0] == cf[2].d[0] &&
-         cf[1].d[1] == cf[2].d[1];
-}
 
 // ---------------------------------------------------- warp reductions ----
 QF_D double warp_sum(double v) {

@@ -72,3 +72,35 @@ def test_qaoa_large_against_oracle():
     cuts = orc.graph_cuts(n, g.edges())
     assert abs(prob.expectation(beta, gamma) - orc.expectation(ref, cuts)) < 1e-10
     assert prob.maxcut == cuts.max()
+
+
+@pytest.mark.parametrize("arith", ["ff", "fp64", "c64"])
+@pytest.mark.parametrize("n,p", [(7, 2), (8, 3), (9, 4), (10, 1), (13, 3), (16, 2)])
+def test_warp_qaoa_state_vs_engine_and_oracle(n, p, arith, monkeypatch):
+    """The warp-tile QAOA forward kernel (default; merged layer boundaries,
+    |+>^n generated in the first pass), at each register-bit count, equals
+    the shared-memory engine path and the oracle, with node weights."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    from quantumflow_gb300 import qaoa as qaoa_mod
+    dtype = "complex64" if arith == "c64" else "complex128"
+    if arith != "c64":
+        layout = nat.LAYOUT_C128 if arith == "fp64" else nat.LAYOUT_FF
+        monkeypatch.setattr(qaoa_mod, "compute_layout", lambda d: layout)
+    g = qf.qaoa.gnp_random_graph(n, 0.5, seed=n + p)
+    g.nodes[0]["weight"] = 0.3
+    g.nodes[n - 1]["weight"] = -1.3
+    rng = np.random.default_rng(n * p)
+    beta, gamma = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
+    nw = [g.nodes[q].get("weight", None) for q in range(n)]
+    ref = orc.run_ops(orc.zero_state(n), orc.qubo_ops(n, g.edges(), p, beta, gamma, None, nw)).reshape(-1)
+    tol = 1e-5 if dtype == "complex64" else 1e-12
+    modes = (0, 1, 2, 3) if dtype == "complex128" else (0, 1, 3, 4)
+    try:
+        for mode in modes:
+            nat.call("qf_set_tile_kernel", mode)
+            prob = qf.QAOAMaxCut(g, p, dtype=dtype)
+            st = prob.state(beta, gamma).asarray().reshape(-1)
+            assert np.max(np.abs(st - ref)) < tol, mode
+    finally:
+        nat.call("qf_set_tile_kernel", 0)
