@@ -88,6 +88,11 @@ int qf_timing_enable(int on);
  * thread (the adjoint's warp tiles take 2 or 3 for complex128 and
  * float-float, 3 or 4 for complex64, else their default). */
 int qf_set_tile_kernel(int mode);
+/* Gate merging before pass planning (diagnostics and tests; no reference
+ * counterpart), process-wide: 1 = on (default) -- consecutive gates are
+ * multiplied into blocks of at most two qubits on the host whenever
+ * fusion_k > 1; 0 = every gate is applied as given. */
+int qf_set_gate_merging(int on);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
 
 /* ------------------------------------------------- state preparation ------ */

@@ -13,6 +13,7 @@ extern thread_local int t_last_cuda_error;
 extern int g_force_smem_tile;
 extern int g_adjoint_smem_only;
 extern int g_warp_rb_override;
+extern int g_merge_gates;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
                const double* gamma, const double* node_theta, int fusion_k, cudaStream_t stream);
@@ -94,6 +95,12 @@ int qf_set_tile_kernel(int mode) {
   g_force_smem_tile = mode == 1;
   g_adjoint_smem_only = mode == 1;
   g_warp_rb_override = mode >= 2 ? mode : 0;
+  return QF_OK;
+}
+
+int qf_set_gate_merging(int on) {
+  if (on != 0 && on != 1) return QF_ERR_INVALID_ARGUMENT;
+  g_merge_gates = on;
   return QF_OK;
 }
 

@@ -734,6 +734,31 @@ QF_D void rswap_dispatch(int j, int k, E (&a)[1 << RB]) {
   }
 }
 
+// Exchange lane bit l with register-index bit J: the lane whose bit l is h
+// keeps its registers with bit J = h and trades the others with its partner.
+template <int RB, int J, typename E>
+QF_D void lswap(int l, int lane, E (&a)[1 << RB]) {
+  const bool hi = (lane >> l) & 1;
+#pragma unroll
+  for (int i = 0; i < (1 << (RB - 1)); ++i) {
+    const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
+    const int i1 = i0 | (1 << J);
+    const E x0 = a[i0], x1 = a[i1];
+    const E recv = shfl_xor(hi ? x0 : x1, 1 << l);
+    a[i0] = hi ? recv : x0;
+    a[i1] = hi ? x1 : recv;
+  }
+}
+template <int RB, typename E>
+QF_D void lswap_dispatch(int l, int j, int lane, E (&a)[1 << RB]) {
+  switch (j) {
+    case 0: lswap<RB, 0>(l, lane, a); break;
+    case 1: if constexpr (RB > 1) lswap<RB, 1>(l, lane, a); break;
+    case 2: if constexpr (RB > 2) lswap<RB, 2>(l, lane, a); break;
+    case 3: if constexpr (RB > 3) lswap<RB, 3>(l, lane, a); break;
+  }
+}
+
 template <int RB, typename E>
 QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t xb,
                       const int64_t (&hoff)[1 << RB], E (&a)[1 << RB]) {
@@ -791,9 +816,11 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
     int64_t base = st << 5;
 #pragma unroll
     for (int j = 0; j < RB; ++j) base = insert0(base, P.hb[j]);
-    const int64_t xb = base | lane;
-    // register-index bit j holds global bit (pb >> 8j) & 255
+    // register-index bit j holds global bit (pb >> 8j) & 255, lane bit l
+    // global bit (lm >> 8l) & 255; lx = the lane's share of the global index
     uint32_t pb = pb0;
+    uint64_t lm = 0x0403020100ull;
+    int64_t lx = lane;
     auto offset = [&](int r) {
       int64_t o = 0;
 #pragma unroll
@@ -803,7 +830,7 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
     };
     E a[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[r] = gin[xb | offset(r)];
+    for (int r = 0; r < R; ++r) a[r] = gin[base | lane | offset(r)];
     for (int pc = 0; pc < P.nprog; ++pc) {
       const TInstr in = P.prog[pc];
       switch (in.code) {
@@ -833,13 +860,23 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
           int64_t hoff[R];
 #pragma unroll
           for (int r = 0; r < R; ++r) hoff[r] = offset(r);
-          seg_apply_w<RB>(P, in, scoef, xb, hoff, a);
+          seg_apply_w<RB>(P, in, scoef, base | lx, hoff, a);
+          break;
+        }
+        case I_LSWAP: {
+          lswap_dispatch<RB>(in.a, in.b, lane, a);
+          const uint32_t sl = 8u * in.a, sj = 8u * in.b;
+          const uint32_t gl = (uint32_t)(lm >> sl) & 255u, gj = (pb >> sj) & 255u;
+          lm = (lm & ~(uint64_t(255) << sl)) | (uint64_t(gj) << sl);
+          pb = (pb & ~(255u << sj)) | (gl << sj);
+          lx = (lx & ~(int64_t(1) << gl)) | (int64_t((lane >> in.a) & 1) << gj);
           break;
         }
       }
     }
+    // the program ends with every lane bit back on its own global bit
 #pragma unroll
-    for (int r = 0; r < R; ++r) gout[xb | offset(r)] = a[r];
+    for (int r = 0; r < R; ++r) gout[base | lane | offset(r)] = a[r];
   }
 }
 
@@ -1390,19 +1427,33 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
     const HostOp& op = ops[i];
     if (is_elementwise(op.type)) continue;
     if (op.type != OP_DENSE1 && op.type != OP_DENSE2) return QF_ERR_NOT_SUPPORTED;
+    if (op.type == OP_DENSE2 && RB < 2) return QF_ERR_NOT_SUPPORTED;
     for (int j = 0; j < op.k; ++j)
       if (op.gb[j] >= 5 && std::find(hb.begin(), hb.end(), op.gb[j]) == hb.end()) hb.push_back(op.gb[j]);
-    if (op.type == OP_DENSE2 && (op.gb[0] < 5 || op.gb[1] < 5)) return QF_ERR_NOT_SUPPORTED;
   }
   if ((int)hb.size() > RB) return QF_ERR_NOT_SUPPORTED;
   for (int b = 5; b < n && (int)hb.size() < RB; ++b)
     if (std::find(hb.begin(), hb.end(), b) == hb.end()) hb.push_back(b);
   std::sort(hb.begin(), hb.end());
   for (int j = 0; j < RB; ++j) P.hb[j] = (uint8_t)hb[j];
-  auto reg_of = [&](int b) { return (int)(std::find(hb.begin(), hb.end(), b) - hb.begin()); };
-  // pos[h]: register-index bit currently holding hb[h]; swaps bring a
-  // gate's bit to the top register bit (and a 2-qubit gate's LSB below it)
-  int pos[4] = {0, 1, 2, 3}, at[4] = {0, 1, 2, 3};
+  // where each global bit of the sub-tile lives while the program runs:
+  // reg[p] = global bit of register-index bit p, lanes[l] = of lane bit l.
+  // Register exchanges (SWAP kernels) bring a gate's bit to the top register
+  // bit (a 2-qubit gate's LSB below it); lane exchanges bring a lane bit of
+  // a 2-qubit gate into the registers, and the program ends with the lanes
+  // restored (coalesced stores).
+  int reg[4] = {0, 0, 0, 0}, lanes[5] = {0, 1, 2, 3, 4};
+  for (int j = 0; j < RB; ++j) reg[j] = hb[j];
+  auto reg_pos = [&](int g) {
+    for (int j = 0; j < RB; ++j)
+      if (reg[j] == g) return j;
+    return -1;
+  };
+  auto lane_pos = [&](int g) {
+    for (int l = 0; l < 5; ++l)
+      if (lanes[l] == g) return l;
+    return -1;
+  };
   // element-wise coefficients first (staged in shared memory), then dense
   int nc = 0, nprog = 0, nseg = 0;
   std::vector<int> coef_at(idx.size(), 0);
@@ -1435,9 +1486,34 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
     }
     if (pass == 0) P.necoef = nc;
   }
-  for (size_t i = 0; i < idx.size(); ++i) {
+  bool ok = true;
+  auto emit = [&](TInstr t) {
+    if (nprog >= 160) {
+      ok = false;
+      return;
+    }
+    P.prog[nprog++] = t;
+  };
+  auto rswap = [&](int j, int target) {  // exchange register-index bits j and target
+    if (j == target) return;
+    const int lo = j < target ? j : target, hi = j < target ? target : j;
+    emit(TInstr{I_RSWAP, (uint8_t)lo, (uint8_t)hi, 0, 0, 0});
+    std::swap(reg[j], reg[target]);
+  };
+  auto lswap = [&](int l, int j) {  // exchange lane bit l with register-index bit j
+    emit(TInstr{I_LSWAP, (uint8_t)l, (uint8_t)j, 0, 0, 0});
+    std::swap(lanes[l], reg[j]);
+  };
+  // bring global bit g into the registers, not evicting global bit keep
+  auto to_reg = [&](int g, int keep) {
+    if (reg_pos(g) >= 0) return;
+    const int l = lane_pos(g);
+    int j = SWAP ? RB - 1 : 0;
+    if (reg[j] == keep) j = SWAP ? RB - 2 : 1;
+    lswap(l, j);
+  };
+  for (size_t i = 0; i < idx.size() && ok; ++i) {
     const HostOp& op = ops[idx[i]];
-    if (nprog >= 160) return QF_ERR_NOT_SUPPORTED;
     if (is_elementwise(op.type)) {
       if (nseg >= 64) return QF_ERR_NOT_SUPPORTED;
       SegOp& so = P.segs[nseg];
@@ -1454,39 +1530,38 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
           P.prog[nprog - 1].a + P.prog[nprog - 1].b == nseg) {
         P.prog[nprog - 1].b++;
       } else {
-        P.prog[nprog++] = TInstr{I_SEG, (uint8_t)nseg, 1, 0, 0, 0};
+        emit(TInstr{I_SEG, (uint8_t)nseg, 1, 0, 0, 0});
       }
       ++nseg;
-    } else {
-      auto bring = [&](int h, int target) -> bool {  // move hb[h] to register bit `target`
-        const int j = pos[h];
-        if (!SWAP || j == target) return true;
-        if (nprog >= 159) return false;
-        const int lo = j < target ? j : target, hi = j < target ? target : j;
-        P.prog[nprog++] = TInstr{I_RSWAP, (uint8_t)lo, (uint8_t)hi, 0, 0, 0};
-        const int other = at[target];
-        at[target] = h;
-        at[j] = other;
-        pos[h] = target;
-        pos[other] = j;
-        return true;
-      };
-      if (op.type == OP_DENSE1) {
-        const int b = op.gb[0];
-        if (b < 5) {
-          P.prog[nprog++] = TInstr{I_G1L, (uint8_t)b, 0, 0, (uint16_t)coef_at[i], 0};
-        } else {
-          if (!bring(reg_of(b), RB - 1)) return QF_ERR_NOT_SUPPORTED;
-          P.prog[nprog++] = TInstr{I_G1R, (uint8_t)(SWAP ? 0 : reg_of(b)), 0, 0, (uint16_t)coef_at[i], 0};
-        }
+    } else if (op.type == OP_DENSE1) {
+      const int g = op.gb[0];
+      const int l = lane_pos(g);
+      if (l >= 0) {
+        emit(TInstr{I_G1L, (uint8_t)l, 0, 0, (uint16_t)coef_at[i], 0});
       } else {
-        if (RB < 2) return QF_ERR_NOT_SUPPORTED;
-        if (!bring(reg_of(op.gb[0]), RB - 1) || !bring(reg_of(op.gb[1]), RB - 2)) return QF_ERR_NOT_SUPPORTED;
-        P.prog[nprog++] = TInstr{I_G2R, (uint8_t)(SWAP ? 0 : reg_of(op.gb[0])),
-                                 (uint8_t)(SWAP ? 0 : reg_of(op.gb[1])), 0, (uint16_t)coef_at[i], 0};
+        if (SWAP) rswap(reg_pos(g), RB - 1);
+        emit(TInstr{I_G1R, (uint8_t)(SWAP ? 0 : reg_pos(g)), 0, 0, (uint16_t)coef_at[i], 0});
       }
+    } else {
+      const int g0 = op.gb[0], g1 = op.gb[1];
+      to_reg(g0, g1);
+      to_reg(g1, g0);
+      if (SWAP) {
+        rswap(reg_pos(g0), RB - 1);
+        rswap(reg_pos(g1), RB - 2);
+      }
+      emit(TInstr{I_G2R, (uint8_t)(SWAP ? 0 : reg_pos(g0)), (uint8_t)(SWAP ? 0 : reg_pos(g1)), 0,
+                  (uint16_t)coef_at[i], 0});
     }
   }
+  // restore the lanes in order; a lane fixed here stays fixed (the bit
+  // fetched for lane l is never in a lane < l)
+  for (int l = 0; l < 5 && ok; ++l) {
+    if (lanes[l] == l) continue;
+    if (reg_pos(l) < 0) lswap(lane_pos(l), SWAP ? RB - 1 : 0);
+    lswap(l, reg_pos(l));
+  }
+  if (!ok) return QF_ERR_NOT_SUPPORTED;
   P.nprog = nprog;
   const size_t smem = (size_t)P.necoef * sizeof(Coef);
   static std::atomic<bool> attr[64];
@@ -1530,16 +1605,172 @@ int launch_tile_block(const void* in, void* out, int n, int layout, const std::v
   return QF_ERR_LAYOUT;
 }
 
+// ------------------------------------------------------- gate merging ----
+// Consecutive gates are multiplied into blocks of at most two qubits on the
+// host (in double precision) before the passes are planned: a 1-qubit gate
+// joins the last gate on its qubit when that gate is dense (a product costs
+// nothing extra), and a 2-qubit gate absorbs the pending 1-qubit gates on
+// its qubits when it is dense or when both qubits have one (a diagonal CZ
+// between two dense layers becomes one dense 4x4 instead of two 2x2 gates
+// and a sign).  Only gates that commute are reordered: a gate moves past
+// another only when they share no qubit.
+static bool mergeable(const HostOp& op) {
+  switch (op.type) {
+    case OP_DENSE1:
+    case OP_DENSE2:
+      return true;
+    case OP_DIAG:
+    case OP_SIGN:
+    case OP_MONO:
+      return op.k <= 2;
+  }
+  return false;
+}
+
+static std::vector<cplx> dense_of(const HostOp& op) {
+  const int G = 1 << op.k;
+  if ((int)op.m.size() == G * G) return op.m;
+  std::vector<cplx> m((size_t)G * G, cplx(0, 0));
+  if (op.type == OP_DIAG) {
+    for (int r = 0; r < G; ++r) m[r * G + r] = op.diag[r];
+  } else if (op.type == OP_SIGN) {
+    for (int r = 0; r < G; ++r) m[r * G + r] = r == G - 1 ? cplx(-1, 0) : cplx(1, 0);
+  } else if (op.type == OP_MONO) {
+    for (int r = 0; r < G; ++r) m[r * G + op.perm[r]] = op.diag[r];
+  }
+  return m;
+}
+
+// the matrix of `op` (k = 1 or 2) acting on the bits `bits` (MSB first, 2 bits)
+static std::vector<cplx> embed2(const HostOp& op, const int bits[2]) {
+  const std::vector<cplx> m = dense_of(op);
+  std::vector<cplx> e(16, cplx(0, 0));
+  if (op.k == 1) {
+    const bool msb = op.gb[0] == bits[0];
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        const int rs = msb ? r >> 1 : r & 1, cs = msb ? c >> 1 : c & 1;  // acted-on bit
+        const int ro = msb ? r & 1 : r >> 1, co = msb ? c & 1 : c >> 1;  // other bit
+        if (ro == co) e[r * 4 + c] = m[rs * 2 + cs];
+      }
+    return e;
+  }
+  if (op.gb[0] == bits[0]) return m;
+  auto sw = [](int v) { return ((v & 1) << 1) | (v >> 1); };  // exchange the two index bits
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) e[r * 4 + c] = m[sw(r) * 4 + sw(c)];
+  return e;
+}
+
+static std::vector<cplx> matmul_n(const std::vector<cplx>& a, const std::vector<cplx>& b, int G) {
+  std::vector<cplx> c((size_t)G * G, cplx(0, 0));
+  for (int i = 0; i < G; ++i)
+    for (int k = 0; k < G; ++k) {
+      const cplx v = a[i * G + k];
+      if (v == cplx(0, 0)) continue;
+      for (int j = 0; j < G; ++j) c[i * G + j] += v * b[k * G + j];
+    }
+  return c;
+}
+
+// rebuild `op` as the gate with matrix m on bits (k = 1 or 2), re-classified
+static void set_matrix(HostOp& op, int k, const int* bits, const std::vector<cplx>& m) {
+  std::vector<double> flat(2 * m.size());
+  for (size_t i = 0; i < m.size(); ++i) {
+    flat[2 * i] = m[i].real();
+    flat[2 * i + 1] = m[i].imag();
+  }
+  HostOp r;
+  classify_op(k, bits, flat.data(), r);
+  op = r;
+}
+
+static bool dense_cost(const HostOp& op) { return op.type == OP_DENSE1 || op.type == OP_DENSE2; }
+
+void merge_ops(std::vector<HostOp>& ops, int n) {
+  std::vector<HostOp> out;
+  std::vector<char> alive;
+  std::vector<int> last(n, -1);
+  out.reserve(ops.size());
+  for (HostOp& o : ops) {
+    if (!mergeable(o)) {
+      const int idx = (int)out.size();
+      if (o.type == OP_CUT || o.type == OP_PHASE) {
+        for (int q = 0; q < n; ++q) last[q] = idx;
+      } else {
+        for (int j = 0; j < o.k; ++j) last[o.gb[j]] = idx;
+      }
+      out.push_back(std::move(o));
+      alive.push_back(1);
+      continue;
+    }
+    if (o.k == 1) {
+      const int q = o.gb[0];
+      const int t = last[q];
+      if (t >= 0 && alive[t] && mergeable(out[t]) && (dense_cost(out[t]) || out[t].k == 1)) {
+        HostOp& d = out[t];
+        if (d.k == 1) {
+          const int bits[1] = {q};
+          set_matrix(d, 1, bits, matmul_n(dense_of(o), dense_of(d), 2));
+        } else {
+          const int bits[2] = {d.gb[0], d.gb[1]};
+          set_matrix(d, 2, bits, matmul_n(embed2(o, bits), dense_of(d), 4));
+        }
+        continue;
+      }
+      last[q] = (int)out.size();
+      out.push_back(std::move(o));
+      alive.push_back(1);
+      continue;
+    }
+    // two qubits
+    const int a = o.gb[0], b = o.gb[1];
+    const int bits[2] = {a, b};
+    const int ta = last[a], tb = last[b];
+    if (ta >= 0 && ta == tb && alive[ta] && mergeable(out[ta]) && out[ta].k == 2) {
+      HostOp& d = out[ta];
+      const int dbits[2] = {d.gb[0], d.gb[1]};
+      set_matrix(d, 2, dbits, matmul_n(embed2(o, dbits), dense_of(d), 4));
+      continue;
+    }
+    std::vector<cplx> m = dense_of(o);
+    auto pending = [&](int t) {  // a live 1-qubit gate that is the last on its qubit
+      return t >= 0 && alive[t] && mergeable(out[t]) && out[t].k == 1;
+    };
+    const bool pa = pending(ta), pb = pending(tb);
+    const bool cheap_a = pa && !dense_cost(out[ta]), cheap_b = pb && !dense_cost(out[tb]);
+    const bool take_all = dense_cost(o) || (pa && pb);
+    if (pa && (take_all || cheap_a)) {
+      m = matmul_n(m, embed2(out[ta], bits), 4);
+      alive[ta] = 0;
+    }
+    if (pb && (take_all || cheap_b)) {
+      m = matmul_n(m, embed2(out[tb], bits), 4);
+      alive[tb] = 0;
+    }
+    HostOp r;
+    set_matrix(r, 2, bits, m);
+    last[a] = last[b] = (int)out.size();
+    out.push_back(std::move(r));
+    alive.push_back(1);
+  }
+  ops.clear();
+  for (size_t i = 0; i < out.size(); ++i)
+    if (alive[i]) ops.push_back(std::move(out[i]));
+}
+
 // Greedy fusion: walk the ops in order; element-wise ops join the current
 // block unconditionally (they need no tile bits), every other op joins while
 // the union of high bits (>= Lmin) stays within fusion_k.
 int g_default_fusion[3] = {4, 2, 2};  // per layout (C64, C128, FF): warp-tile capacity
+int g_merge_gates = 1;                 // qf_set_gate_merging
 
 int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
             cudaStream_t stream, int* passes_out) {
   const int Lmin = 5;  // bits 0..4 are the lane bits of every fused kernel
   if (fusion_k <= 0) fusion_k = g_default_fusion[layout];
   if (fusion_k > 8) fusion_k = 8;
+  if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
   int passes = 0;
   const void* src = in;
   struct Block {

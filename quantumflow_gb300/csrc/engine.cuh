@@ -52,6 +52,7 @@ enum TInstrCode : uint8_t {
   I_SEG = 5,   // a: first SegOp, b: count (element-wise ops in registers)
   I_SMEM = 6,  // a: index into ops[] -- applied in shared memory
   I_RSWAP = 7, // a, b: exchange register-index bits a and b (k_warp)
+  I_LSWAP = 8, // a: lane bit, b: register-index bit; exchange the global bits they hold (k_warp)
 };
 struct TInstr {
   uint8_t code, a, b, c;

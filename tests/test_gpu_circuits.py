@@ -136,3 +136,69 @@ def test_large_round_trip(N):
         assert abs(float(probs.reshape(-1)[0]) - 1) < tol * 10
         del ket, back, probs
         torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("N", [9, 12, 17])
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+@pytest.mark.parametrize("fusion_k", [0, 3])
+def test_gate_merging_equals_unmerged_and_oracle(N, dtype, fusion_k, tile_kernel):
+    """Host gate merging (blocks of <= 2 qubits) and the warp kernel's lane
+    exchanges for 2-qubit gates on lane bits: the merged run equals the
+    unmerged run and the oracle."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(100 + N)
+    circ = qf.Circuit()
+    for layer in range(4):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+        circ += qf.random_gate([0, 3], random_state=rng)          # two lane bits
+        circ += qf.random_gate([N - 2, 1], random_state=rng)      # high, lane
+        circ += qf.random_gate([4, N - 1], random_state=rng)      # lane, high
+        circ += qf.CNOT(2, N - 3)
+        circ += qf.SWAP(1, N - 4)
+        circ += qf.RZ(0.4, 3)
+        circ += qf.X(N - 5)
+        circ += qf.ZZ(0.7, 0, 4)
+        circ += qf.T(N - 1)
+    tol = 1e-12 if dtype == "complex128" else 2e-5
+    try:
+        nat.call("qf_set_gate_merging", 1)
+        merged = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k).asarray().reshape(-1)
+        nat.call("qf_set_gate_merging", 0)
+        plain = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k).asarray().reshape(-1)
+    finally:
+        nat.call("qf_set_gate_merging", 1)
+    assert np.max(np.abs(merged - plain)) < tol
+    if N <= 12:
+        ops = [(g.asoperator(), tuple(g.qubits)) for g in circ]
+        ref = orc.run_ops(orc.zero_state(N), ops).reshape(-1)
+        assert np.max(np.abs(merged - ref)) < tol
+
+
+def test_gate_merging_random_layers_n20():
+    """The random-layer workload (Haar U(2) on every qubit, CZ on a matching)
+    merged vs unmerged at N=20, complex128 and complex64."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    N = 20
+    rng = np.random.default_rng(5)
+    circ = qf.Circuit()
+    for layer in range(6):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    for dtype, tol in (("complex128", 1e-12), ("complex64", 2e-5)):
+        try:
+            nat.call("qf_set_gate_merging", 1)
+            merged = circ.run(qf.zero_state(N, dtype=dtype)).asarray().reshape(-1)
+            nat.call("qf_set_gate_merging", 0)
+            plain = circ.run(qf.zero_state(N, dtype=dtype)).asarray().reshape(-1)
+        finally:
+            nat.call("qf_set_gate_merging", 1)
+        assert np.max(np.abs(merged - plain)) < tol
