@@ -797,25 +797,62 @@ QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, 
 // register bit and the host inserts register-bit exchanges (small code,
 // for the long float-float gate bodies); SWAP = false: one variant per
 // register bit (no exchanges; for the short FP32 bodies).
+constexpr int WARP_STAGES = 3;  // per-warp prefetch ring depth (sub-tiles)
+
+template <int LAY, int RB>
+constexpr size_t warp_ring_bytes() {
+  return (size_t)8 * WARP_STAGES * (32 << RB) * sizeof(typename Types<LAY>::E);
+}
+
 template <int LAY, int RB, bool SWAP>
 __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams P) {
   using E = typename Types<LAY>::E;
   constexpr int R = 1 << RB;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   Coef* scoef = reinterpret_cast<Coef*>(smem_raw);
   for (int i = threadIdx.x; i < P.necoef; i += blockDim.x) scoef[i] = P.coef[i];
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // this warp's ring of prefetched sub-tiles: [stage][register][lane]
+  E* ring = reinterpret_cast<E*>(smem_raw + (((size_t)P.necoef * sizeof(Coef) + 127) & ~size_t(127))) +
+            (size_t)warp * WARP_STAGES * R * 32;
   const int64_t nsub = int64_t(1) << (P.n - 5 - RB);
   const int64_t wstride = (int64_t)gridDim.x * (blockDim.x >> 5);
   const E* gin = reinterpret_cast<const E*>(P.in);
   E* gout = reinterpret_cast<E*>(P.out);
   const uint32_t pb0 = (uint32_t)P.hb[0] | ((uint32_t)P.hb[1] << 8) | ((uint32_t)P.hb[2] << 16) |
                        ((uint32_t)P.hb[3] << 24);
-  for (int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); st < nsub; st += wstride) {
+  int64_t hoff0[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    int64_t o = 0;
+#pragma unroll
+    for (int j = 0; j < RB; ++j)
+      if ((r >> j) & 1) o |= int64_t(1) << P.hb[j];
+    hoff0[r] = o;
+  }
+  auto sub_base = [&](int64_t st) {
     int64_t base = st << 5;
 #pragma unroll
     for (int j = 0; j < RB; ++j) base = insert0(base, P.hb[j]);
+    return base;
+  };
+  auto issue = [&](int64_t st, int sg) {
+    if (st < nsub) {
+      const int64_t xb = sub_base(st) | lane;
+      E* sp = ring + (size_t)sg * R * 32 + lane;
+#pragma unroll
+      for (int r = 0; r < R; ++r) cp_async_amp(sp + r * 32, gin + (xb | hoff0[r]));
+    }
+    cp_async_commit();
+  };
+  int64_t st = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  __syncthreads();  // coefficient table staged
+#pragma unroll
+  for (int k = 0; k < WARP_STAGES - 1; ++k) issue(st + k * wstride, k);
+  int sg = 0;
+  for (; st < nsub; st += wstride) {
+    cp_async_wait<WARP_STAGES - 2>();
+    const int64_t base = sub_base(st);
     // register-index bit j holds global bit (pb >> 8j) & 255, lane bit l
     // global bit (lm >> 8l) & 255; lx = the lane's share of the global index
     uint32_t pb = pb0;
@@ -829,8 +866,14 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
       return o;
     };
     E a[R];
+    {
+      const E* sp = ring + (size_t)sg * R * 32 + lane;
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[r] = gin[base | lane | offset(r)];
+      for (int r = 0; r < R; ++r) a[r] = sp[r * 32];
+    }
+    // refill the stage read one iteration ago (its values are in registers)
+    issue(st + (WARP_STAGES - 1) * wstride, sg == 0 ? WARP_STAGES - 1 : sg - 1);
+    sg = sg + 1 == WARP_STAGES ? 0 : sg + 1;
     for (int pc = 0; pc < P.nprog; ++pc) {
       const TInstr in = P.prog[pc];
       switch (in.code) {
@@ -878,6 +921,7 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
 #pragma unroll
     for (int r = 0; r < R; ++r) gout[base | lane | offset(r)] = a[r];
   }
+  cp_async_wait<0>();
 }
 
 // ============================================================== host side
@@ -1291,7 +1335,15 @@ static int set_smem_attr(K kernel, std::atomic<bool>* flags) {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !flags[dev].load()) {
-    int rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    // the opt-in maximum less the kernel's static shared memory
+    int optin = 0;
+    int rc = check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (rc) return rc;
+    cudaFuncAttributes fa;
+    rc = check_cuda(cudaFuncGetAttributes(&fa, kernel));
+    if (rc) return rc;
+    rc = check_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         optin - (int)fa.sharedSizeBytes));
     if (rc) return rc;
     flags[dev].store(true);
   }
@@ -1563,7 +1615,7 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
   }
   if (!ok) return QF_ERR_NOT_SUPPORTED;
   P.nprog = nprog;
-  const size_t smem = (size_t)P.necoef * sizeof(Coef);
+  const size_t smem = (((size_t)P.necoef * sizeof(Coef) + 127) & ~size_t(127)) + warp_ring_bytes<LAY, RB>();
   static std::atomic<bool> attr[64];
   int rc = set_smem_attr(k_warp<LAY, RB, SWAP>, attr);
   if (rc) return rc;
