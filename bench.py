@@ -62,13 +62,21 @@ def build_circuit(ops):
     return circ
 
 
-def warp_traffic(N, S):
-    """DRAM bytes per fused-pass launch: read + write measured by ncu on the
-    same kernel at N=24 complex128 (268.6 MB + 207.2 MB; the write shortfall
-    is dirty L2 at kernel end), scaled by the state size to N qubits."""
-    if S != 16:
+# DRAM bytes (read, write) per launch measured by ncu on the random-layer
+# workload at N=24 complex128 (profiles/); the write shortfall is dirty L2
+# lines still resident when the kernel ends.  Scaled by the state size.
+KERNEL_TRAFFIC_N24 = {
+    "dense2": (268.476160e6, 206.269696e6),
+    "warp_tile": (268.558592e6, 207.177984e6),
+}
+
+
+def kernel_traffic(kind, N, S):
+    """ncu-measured DRAM bytes per launch of `kind`, scaled to N qubits."""
+    if S != 16 or kind not in KERNEL_TRAFFIC_N24:
         return None
-    return (268.558592e6 + 207.177984e6) * 2 ** (N - 24)
+    rd, wr = KERNEL_TRAFFIC_N24[kind]
+    return (rd + wr) * 2 ** (N - 24)
 
 
 def measured_peaks():
@@ -360,7 +368,7 @@ def main():
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
         "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-        "traffic": warp_traffic(N, S) if dom == "warp_tile" else None, "launches_timed": dom_n,
+        "traffic": kernel_traffic(dom, N, S), "launches_timed": dom_n,
         "share_of_kernel_time": dom_ms / total_kernel_ms if total_kernel_ms else None,
         "bytes_per_launch": sweep_bytes,
     }

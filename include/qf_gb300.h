@@ -238,6 +238,12 @@ int qf_expectation_cuts_noalloc(const void* psi, int n, int layout, const uint16
 /* out[0] = sum_x diag[x] |psi_x|^2 for a real device array diag[2^n]. */
 int qf_expectation_diag(const void* psi, int n, int layout, const double* diag, double* out,
                         void* workspace, size_t workspace_bytes, void* stream);
+/* out[0] = probability that the qubit on reference axis `axis` reads 0,
+ * out[1] = that it reads 1 (unnormalised: their sum is the squared norm).
+ * Replaces the projected copy + norm of Measure.run,
+ * quantumflow/stdops.py:53-54 (prob_zero = P0(qubit).run(ket).norm()). */
+int qf_qubit_probabilities(const void* psi, int n, int layout, int axis, double* out, void* workspace,
+                           size_t workspace_bytes, void* stream);
 /* out[0] = sum_x |psi_x|^2 (quantumflow/qubits.py:180-182 norm). */
 int qf_norm2(const void* psi, int n, int layout, double* out, void* workspace,
              size_t workspace_bytes, void* stream);

@@ -126,6 +126,59 @@ def CNOT():
     return np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=np.complex128)
 
 
+def S():
+    """quantumflow/stdgates.py:112-125."""
+    return np.array([[1, 0], [0, 1j]], dtype=np.complex128)
+
+
+def PHASE(theta):
+    """quantumflow/stdgates.py:154-166."""
+    return np.array([[1, 0], [0, cis(theta)]], dtype=np.complex128)
+
+
+def RY(theta):
+    """quantumflow/stdgates.py:208-224."""
+    c, s = np.cos(theta / 2), np.sin(theta / 2)
+    return np.array([[c, -s], [s, c]], dtype=np.complex128)
+
+
+def SWAP():
+    """quantumflow/stdgates.py:315-338."""
+    return np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], dtype=np.complex128)
+
+
+def ISWAP():
+    """quantumflow/stdgates.py:341-362."""
+    return np.array([[1, 0, 0, 0], [0, 0, 1j, 0], [0, 1j, 0, 0], [0, 0, 0, 1]], dtype=np.complex128)
+
+
+def CPHASE(theta):
+    """quantumflow/stdgates.py:431-446: diag(1, 1, 1, e^{i theta})."""
+    return np.diag([1, 1, 1, cis(theta)]).astype(np.complex128)
+
+
+def CCNOT():
+    """quantumflow/stdgates.py:519-556: Toffoli, control qubits first."""
+    m = np.eye(8, dtype=np.complex128)
+    m[6:, 6:] = [[0, 1], [1, 0]]
+    return m
+
+
+NAMED = {"H": H, "X": X, "T": T, "S": S, "RX": RX, "RY": RY, "RZ": RZ, "PHASE": PHASE, "CNOT": CNOT,
+         "CZ": CZ, "SWAP": SWAP, "CPHASE": CPHASE, "ZZ": ZZ, "ISWAP": ISWAP, "CCNOT": CCNOT}
+
+
+def program_ops(names, params, qubits):
+    """Gate list of a program of named-gate calls (quantumflow/programs.py
+    Call.run :429-439: the named gate class, its parameters, its qubits)."""
+    ops = []
+    for name, ps, qs in zip(names, params, qubits):
+        ps = [p for p in ps if not np.isnan(p)]
+        qs = [int(q) for q in qs if q >= 0]
+        ops.append((NAMED[str(name)](*ps), tuple(qs)))
+    return ops
+
+
 # ------------------------------------------------------------- QAOA --------
 def qubo_ops(n, edges, p, beta, gamma, weights=None, node_weights=None):
     """Gate list of quantumflow/qaoa.py:22-64 qubo_circuit for nodes 0..n-1:

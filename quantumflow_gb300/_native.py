@@ -91,6 +91,7 @@ SIGNATURES = {
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),
     "qf_expectation_cuts_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
     "qf_norm2": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _sz, _vp]),
+    "qf_qubit_probabilities": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _sz, _vp]),
     "qf_inner": (_c_int, [_vp, _vp, _c_int, _c_int, _vp, _vp, _sz, _vp]),
     "qf_probabilities": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
     "qf_sample": (_c_int, [_vp, _c_int, _c_int, _c_i64, _c_u64, _vp, _vp, _sz, _vp]),

@@ -94,8 +94,19 @@ class Circuit(Operation):
             ket = zero_state(self.qubits)
         flat = self.gates()
         if any(not isinstance(g, Gate) for g in flat):
-            for elem in flat:  # mixed operations: run one at a time
+            # mixed operations: each run of consecutive gates is one fused
+            # launch, other operations run on their own in between
+            pending = []
+            for elem in flat:
+                if isinstance(elem, Gate):
+                    pending.append(elem)
+                    continue
+                if pending:
+                    ket = Circuit(pending).run(ket, fusion_k)
+                    pending = []
                 ket = elem.run(ket)
+            if pending:
+                ket = Circuit(pending).run(ket, fusion_k)
             return ket
         op_k, op_axes, op_mats, nops = self.packed(ket.qubits)
         src = ket.buffer.compute()

@@ -181,13 +181,28 @@ __device__ void tile_apply_b(const TileOpsB& T, E* sp, E* sl, const uint16_t* sc
     }
     __syncthreads();
   }
-  // mixer gradient terms for this pass's bits, then undo RX on them
+  // mixer gradient terms for this pass's bits, then undo RX on them.  In
+  // FP32 arithmetic each thread sums its few pairs of one bit in FP32 and
+  // folds the partial into the compensated accumulator once per bit.
   for (int i = 0; i < T.nbits; ++i) {
     const int q = T.lbits[i], bit = 1 << q;
-    for (int pr = tid; pr < (N >> 1); pr += nthr) {
-      const int i0 = ((pr >> q) << (q + 1)) | (pr & (bit - 1));
-      imconj(accx, sl[i0], sp[i0 | bit], 1.f);
-      imconj(accx, sl[i0 | bit], sp[i0], 1.f);
+    if constexpr (sizeof(E) == sizeof(float2)) {
+      float part = 0.f;
+      for (int pr = tid; pr < (N >> 1); pr += nthr) {
+        const int i0 = ((pr >> q) << (q + 1)) | (pr & (bit - 1));
+        const float2 l0 = sl[i0], l1 = sl[i0 | bit], p0 = sp[i0], p1 = sp[i0 | bit];
+        part = fmaf(l0.x, p1.y, part);
+        part = fmaf(-l0.y, p1.x, part);
+        part = fmaf(l1.x, p0.y, part);
+        part = fmaf(-l1.y, p0.x, part);
+      }
+      accx.add(part, 0.f);
+    } else {
+      for (int pr = tid; pr < (N >> 1); pr += nthr) {
+        const int i0 = ((pr >> q) << (q + 1)) | (pr & (bit - 1));
+        imconj(accx, sl[i0], sp[i0 | bit], 1.f);
+        imconj(accx, sl[i0 | bit], sp[i0], 1.f);
+      }
     }
   }
   __syncthreads();
@@ -201,12 +216,19 @@ __device__ void tile_apply_b(const TileOpsB& T, E* sp, E* sl, const uint16_t* sc
     __syncthreads();
   }
   if (T.phase) {  // cost-layer gradient, then undo the phase
+    float part = 0.f;
     for (int x = tid; x < N; x += nthr) {
       const float c = (float)sc[x];
-      imconj(acccut, sl[x], sp[x], half_e - c);
+      if constexpr (sizeof(E) == sizeof(float2)) {
+        const float2 l = sl[x], v = sp[x];
+        part = fmaf(half_e - c, fmaf(l.x, v.y, -l.y * v.x), part);
+      } else {
+        imconj(acccut, sl[x], sp[x], half_e - c);
+      }
       sp[x] = cmulc(phase_tab[sc[x]], sp[x]);
       sl[x] = cmulc(phase_tab[sc[x]], sl[x]);
     }
+    if constexpr (sizeof(E) == sizeof(float2)) acccut.add(part, 0.f);
     __syncthreads();
   }
 }

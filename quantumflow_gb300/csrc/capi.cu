@@ -290,6 +290,16 @@ int qf_expectation_diag(const void* psi, int n, int layout, const double* diag, 
                      as_stream(stream));
 }
 
+int qf_qubit_probabilities(const void* psi, int n, int layout, int axis, double* out, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  int rc = check_state(psi, n, layout);
+  if (rc) return rc;
+  if (out == nullptr || axis < 0 || axis >= n) return QF_ERR_INVALID_ARGUMENT;
+  rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
+  if (rc) return rc;
+  return reduce_bit(psi, n, layout, n - 1 - axis, out, reinterpret_cast<double*>(workspace), as_stream(stream));
+}
+
 int qf_norm2(const void* psi, int n, int layout, double* out, void* workspace, size_t workspace_bytes,
              void* stream) {
   int rc = check_state(psi, n, layout);

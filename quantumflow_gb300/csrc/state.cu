@@ -186,6 +186,24 @@ __global__ void __launch_bounds__(256) k_reduce_inner(const typename Types<LAY>:
   block_reduce2(re, im, partials);
 }
 
+// Probabilities of global bit `bit` being 0 and 1 (the single-qubit
+// measurement of quantumflow/stdops.py:53-64, without the projected copy).
+template <int LAY>
+__global__ void __launch_bounds__(256) k_reduce_bit(const typename Types<LAY>::E* psi, int64_t namps, int bit,
+                                                    double* partials) {
+  FFAcc p0, p1;
+  p0.zero();
+  p1.zero();
+  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < namps; x += nthr) {
+    float ph, pl;
+    norm2_ff(psi[x], ph, pl);
+    if ((x >> bit) & 1) p1.add(ph, pl);
+    else p0.add(ph, pl);
+  }
+  block_reduce2(p0, p1, partials);
+}
+
 // Fixed-order final pass over the block partials.
 __global__ void k_finish2(const double* partials, int nblocks, double* out, int nout) {
   __shared__ double sh[2][256];
@@ -231,6 +249,25 @@ static int reduce_diag_t(const void* psi, int n, int kind, const uint16_t* cuts,
   else k_reduce_diag<LAY, 2><<<nb, 256, 0, stream>>>(p, namps, cuts, diag, partials);
   k_finish2<<<1, 256, 0, stream>>>(partials, nb, out, 1);
   return check_cuda(cudaGetLastError());
+}
+
+template <int LAY>
+static int reduce_bit_t(const void* psi, int n, int bit, double* out, double* partials, cudaStream_t stream) {
+  using E = typename Types<LAY>::E;
+  const int64_t namps = int64_t(1) << n;
+  const int nb = reduce_blocks(namps);
+  k_reduce_bit<LAY><<<nb, 256, 0, stream>>>(reinterpret_cast<const E*>(psi), namps, bit, partials);
+  k_finish2<<<1, 256, 0, stream>>>(partials, nb, out, 2);
+  return check_cuda(cudaGetLastError());
+}
+
+int reduce_bit(const void* psi, int n, int layout, int bit, double* out, double* partials, cudaStream_t stream) {
+  switch (layout) {
+    case C64: return reduce_bit_t<C64>(psi, n, bit, out, partials, stream);
+    case C128: return reduce_bit_t<C128>(psi, n, bit, out, partials, stream);
+    case FF: return reduce_bit_t<FF>(psi, n, bit, out, partials, stream);
+  }
+  return QF_ERR_LAYOUT;
 }
 
 int reduce_diag(const void* psi, int n, int layout, int kind, const uint16_t* cuts, const double* diag,

@@ -17,6 +17,7 @@ int reduce_blocks(int64_t namps);
 // kind 0: norm2, 1: uint16 cuts, 2: double diagonal
 int reduce_diag(const void* psi, int n, int layout, int kind, const uint16_t* cuts, const double* diag,
                 double* out, double* partials, cudaStream_t stream);
+int reduce_bit(const void* psi, int n, int layout, int bit, double* out, double* partials, cudaStream_t stream);
 int reduce_inner(const void* a, const void* b, int n, int layout, double* out, double* partials,
                  cudaStream_t stream);
 int probabilities(const void* psi, int n, int layout, double* probs, cudaStream_t stream);

@@ -45,6 +45,12 @@ class Operation(ABC):
     def H(self) -> "Operation":
         raise NotImplementedError()
 
+    def quil(self) -> str:
+        return self.name
+
+    def __str__(self) -> str:
+        return self.quil()
+
 
 class Gate(Operation):
     """A quantum logic gate (quantumflow/ops.py:91-262)."""

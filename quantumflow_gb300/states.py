@@ -306,6 +306,8 @@ def inner(a: State, b: State) -> complex:
 # ----------------------------------------------------------- constructors --
 def basis_state(qubits: Union[int, Qubits], index: int = 0, dtype: str = "complex128") -> State:
     N, qubits = qubits_count_tuple(qubits)
+    if N == 0:  # the empty register: one amplitude, 1 (kept on the host side of the ABI)
+        return State(torch.ones(1, dtype=_DTYPES[dtype], device=_device()), qubits)
     buf = Buffer.empty(N, compute_layout(dtype))
     nat.call("qf_fill_basis", nat.ptr(buf.data), N, buf.layout, int(index), nat.stream_handle(buf.device))
     return State(buf, qubits)

@@ -371,17 +371,55 @@ def qaoa_fixtures(qf, rng):
     return out
 
 
+# --------------------------------------------------------------- programs ----
+PROGRAM_GATES = [("H", 0, 1), ("X", 0, 1), ("T", 0, 1), ("S", 0, 1), ("RX", 1, 1), ("RY", 1, 1),
+                 ("RZ", 1, 1), ("PHASE", 1, 1), ("CNOT", 0, 2), ("CZ", 0, 2), ("SWAP", 0, 2),
+                 ("CPHASE", 1, 2), ("ZZ", 1, 2), ("ISWAP", 0, 2), ("CCNOT", 0, 3)]
+
+
+def program_fixtures(qf, rng):
+    """Reference Program runs: the literal amplitudes of
+    tests/test_programs.py:193-217, and seeded random Call programs run by
+    quantumflow/programs.py:152-171 (Call.run :429-439)."""
+    t = os.path.join(REF, "tests")
+    out = {"wf_true": np.array(_literal_in_function(os.path.join(t, "test_programs.py"),
+                                                      "test_qaoa_circuit", "complex"))}
+    for case, (nq, ncalls) in enumerate([(3, 40), (5, 120), (7, 200)]):
+        names, params, qubits = [], [], []
+        prog = qf.Program()
+        for _ in range(ncalls):
+            name, npar, k = PROGRAM_GATES[rng.integers(len(PROGRAM_GATES))]
+            qs = [int(q) for q in rng.choice(nq, size=k, replace=False)]
+            ps = [float(v) for v in rng.uniform(-np.pi, np.pi, size=npar)]
+            prog += qf.Call(name, ps, qs)
+            names.append(name)
+            params.append(ps + [np.nan] * (1 - len(ps)))
+            qubits.append(qs + [-1] * (3 - len(qs)))
+        ket = prog.run(qf.zero_state(nq))
+        out[f"p{case}_names"] = np.array(names)
+        out[f"p{case}_params"] = np.array(params)
+        out[f"p{case}_qubits"] = np.array(qubits, dtype=np.int64)
+        out[f"p{case}_state"] = ket.tensor.reshape(-1)
+        out[f"p{case}_nq"] = np.array(nq)
+    return out
+
+
 def main():
     qf = import_reference()
     rng = np.random.default_rng(20181203)
     files = {
-        "kat.npz": kat_fixtures(qf),
-        "gates.npz": gate_fixtures(qf),
-        "tensormul.npz": tensormul_fixtures(qf, rng),
-        "circuits.npz": circuit_fixtures(qf, rng),
-        "qaoa.npz": qaoa_fixtures(qf, rng),
+        "kat.npz": lambda: kat_fixtures(qf),
+        "gates.npz": lambda: gate_fixtures(qf),
+        "tensormul.npz": lambda: tensormul_fixtures(qf, rng),
+        "circuits.npz": lambda: circuit_fixtures(qf, rng),
+        "qaoa.npz": lambda: qaoa_fixtures(qf, rng),
+        "programs.npz": lambda: program_fixtures(qf, np.random.default_rng(20181204)),
     }
+    only = set(sys.argv[1:])  # e.g. `programs` to rewrite programs.npz alone
     for fname, arrays in files.items():
+        if only and fname[:-4] not in only:
+            continue
+        arrays = arrays()
         path = os.path.join(HERE, fname)
         np.savez_compressed(path, **arrays)
         print(f"wrote {fname}: {len(arrays)} arrays, {os.path.getsize(path)} bytes")

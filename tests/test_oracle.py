@@ -83,3 +83,15 @@ def test_c1_gradient_ascent(golden):
         gamma, beta = gamma + 0.1 * gg, beta + 0.1 * gb
         traj.append(orc.qaoa_expectation(n, edges, p, beta, gamma))
     np.testing.assert_allclose(traj, q["c1_gd_expectations"], atol=1e-8)
+
+
+def test_oracle_matches_reference_programs(golden):
+    """Seeded Call programs run by the reference's Program.run reproduce in
+    the oracle; the literal amplitudes of its program test agree too."""
+    g = golden["programs"]
+    for case in range(3):
+        nq = int(g[f"p{case}_nq"])
+        ops = orc.program_ops(g[f"p{case}_names"], g[f"p{case}_params"], g[f"p{case}_qubits"])
+        st = orc.run_ops(orc.zero_state(nq), ops).reshape(-1)
+        assert np.max(np.abs(st - g[f"p{case}_state"])) < 1e-12
+    np.testing.assert_allclose(g["wf_true"], golden["kat"]["true_ket"], atol=1e-12)
