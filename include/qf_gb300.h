@@ -187,6 +187,31 @@ int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, int n
                        const double* angles, double* out, int layout, int max_n, int tile_bits, int ctas,
                        void* workspace, size_t workspace_bytes, void* stream);
 
+/* Multi-instance passes for the batch instances too large for one CTA's
+ * shared memory (no reference counterpart: the reference evaluates one
+ * circuit at a time, quantumflow/qaoa.py:22-81).  Each instance keeps psi,
+ * lambda and its cut table in the caller's device workspace; wave w runs
+ * pass w of every instance (forward and adjoint warp-tile passes), so the
+ * launch count is the longest instance's pass count.
+ *   qf_wave_min_qubits: smallest n accepted for `layout` (C64 or FF).
+ *   qf_wave_plan: `instances` is a HOST array (same fields as for
+ *     qf_batch_qaoa_grad; p >= 1, nedges <= 1023).  With host_plan == NULL
+ *     it only reports the host and device bytes needed; otherwise it writes
+ *     the plan into host_plan, which must stay unchanged while it is used.
+ *   qf_wave_prepare: uploads the plan into the device workspace (256-byte
+ *     aligned) and computes the cut tables from the device edge array;
+ *     once per plan, before any stream capture.
+ *   qf_wave_qaoa_grad: one evaluation: out gets, per instance,
+ *     dgamma[p], dbeta[p], <C> at out_offset, from the device angle array.
+ *     No host synchronisation; may be captured in a CUDA graph. */
+int qf_wave_min_qubits(int layout);
+int qf_wave_plan(const qf_batch_instance* instances, int ninstances, int layout, void* host_plan,
+                 size_t host_bytes, size_t* host_bytes_needed, size_t* device_bytes_needed);
+int qf_wave_prepare(const void* host_plan, const uint8_t* edges, void* workspace, size_t workspace_bytes,
+                    void* stream);
+int qf_wave_qaoa_grad(const void* host_plan, void* workspace, size_t workspace_bytes, const double* angles,
+                      double* out, void* stream);
+
 /* ------------------------------------------ learned angle initialiser ----- */
 /* A 3-layer message-passing graph network (hidden width 64, FP32) mapping a
  * graph to 2p QAOA angles (beta_0..beta_{p-1}, gamma_0..gamma_{p-1}); no

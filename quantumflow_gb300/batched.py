@@ -1,9 +1,10 @@
 """Batched QAOA MAXCUT: thousands of uneven instances per launch.
 
 ``QAOABatch`` uploads the instances once (graphs as axis pairs, depths,
-angle and output offsets), orders them largest first, and evaluates every
-instance's <C> and adjoint gradient with one persistent kernel
-(``qf_batch_qaoa_grad``).  The launch (a counter reset plus the kernel) and
+angle and output offsets) and evaluates every instance's <C> and adjoint
+gradient: the instances that fit one CTA's shared memory in one persistent
+kernel (``qf_batch_qaoa_grad``), the larger ones as multi-instance
+warp-tile passes (``qf_wave_qaoa_grad``, one launch per pass index).  The launch (a counter reset plus the kernel) and
 an optional on-device Adam update are captured in a CUDA graph and replayed.
 
 The reference evaluates one circuit at a time (quantumflow/qaoa.py:22-81,
@@ -39,9 +40,12 @@ class QAOABatch:
         dtype: 'complex64' (FP32) or 'complex128' (float-float arithmetic).
         tile_bits, ctas: kernel shape; None takes the autotuned or default
             values (see :mod:`quantumflow_gb300.autotune`).
+        wave_min: smallest n run as multi-instance passes (default: every
+            instance above tile_bits); a larger value keeps more instances in
+            the persistent kernel.
     """
 
-    def __init__(self, graphs, ps, dtype="complex64", tile_bits=None, ctas=None, device=None):
+    def __init__(self, graphs, ps, dtype="complex64", tile_bits=None, ctas=None, device=None, wave_min=None):
         if dtype not in _LAYOUTS:
             raise ValueError("dtype must be complex64 or complex128")
         self.dtype = dtype
@@ -65,8 +69,8 @@ class QAOABatch:
             edges_all.append(np.asarray(edges, dtype=np.uint8).reshape(-1, 2))
         self.max_n = int(self.ns.max()) if self.count else 1
         ts_max = 12 if self.layout == nat.LAYOUT_C64 else 11
-        if self.max_n > 2 * ts_max:
-            raise ValueError(f"instances above {2 * ts_max} qubits are not supported by the batch kernel")
+        if self.max_n > 30:
+            raise ValueError("instances above 30 qubits are not supported by the batched engine")
         # offsets in the caller's (input) order; launch order is largest first
         self.angle_offset = np.concatenate([[0], np.cumsum(2 * self.ps)[:-1]]).astype(np.int64)
         self.out_offset = np.concatenate([[0], np.cumsum(2 * self.ps + 1)[:-1]]).astype(np.int64)
@@ -92,29 +96,60 @@ class QAOABatch:
         self.tile_bits = int(tile_bits if tile_bits is not None else cfg.get("tile_bits", ts_max))
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.ctas = int(ctas if ctas is not None else cfg.get("ctas", 2 * sms))
+        self.wave_min = int(wave_min) if wave_min is not None else 0
         self._alloc_workspace()
         self._graph = None
 
     def _alloc_workspace(self):
-        """Upload the launch order for the current tile size and size the
-        workspace.  Instances with n >= tile_bits + 4 go first, each to a
-        cluster of 8 CTAs; the rest follow, one CTA each; both groups are
-        ordered largest first."""
+        """Split the instances for the current tile size and size both
+        workspaces.  Instances with n <= tile_bits live in one CTA's shared
+        memory (``qf_batch_qaoa_grad``, largest first); the larger ones run
+        as multi-instance warp-tile passes (``qf_wave_qaoa_grad``), which
+        keep psi, lambda and the cut table of each in device memory."""
         self.ctas = max(8, (self.ctas // 8) * 8)
-        coop_min = self.tile_bits + 4
         cost = lambda i: -(2 ** int(self.ns[i])) * (int(self.ps[i]) + 1)
-        large = sorted((i for i in range(self.count) if self.ns[i] >= coop_min), key=lambda i: (cost(i), i))
-        rest = sorted((i for i in range(self.count) if self.ns[i] < coop_min), key=lambda i: (cost(i), i))
+        wmin = max(self.tile_bits + 1, self.wave_min)
+        to_wave = lambda i: self.ns[i] >= wmin and self.ps[i] > 0
+        waves = sorted(i for i in range(self.count) if to_wave(i))
+        # persistent kernel: cluster-shared instances (n >= tile + 4) first,
+        # then the rest, each group largest first
+        coop_min = self.tile_bits + 4
+        large = sorted((i for i in range(self.count) if not to_wave(i) and self.ns[i] >= coop_min),
+                       key=lambda i: (cost(i), i))
+        small = sorted((i for i in range(self.count) if not to_wave(i) and self.ns[i] < coop_min),
+                       key=lambda i: (cost(i), i))
         self.nlarge = len(large)
-        inst = (_Instance * max(1, self.count))()
-        for k, i in enumerate(large + rest):
-            inst[k] = _Instance(int(self.ns[i]), int(self.ps[i]), int(self.nedges[i]), int(self.edge_offset[i]),
-                                int(self.angle_offset[i]), int(self.out_offset[i]))
+        self.nsmall = len(large) + len(small)
+        inst = (_Instance * max(1, self.nsmall))()
+        for k, i in enumerate(large + small):
+            inst[k] = self._inst(i)
         raw = np.frombuffer(bytes(inst), dtype=np.uint8)
         self.d_inst = torch.from_numpy(raw.copy()).to(self.device)
-        self.ws_bytes = nat.lib.qf_batch_workspace_bytes(self.max_n, self.layout, self.ctas)
+        small_n = int(max((self.ns[i] for i in large + small), default=1))
+        self.ws_bytes = nat.lib.qf_batch_workspace_bytes(small_n, self.layout, self.ctas)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=self.device)
+        self.small_max_n = small_n
+        # multi-instance passes
+        self.nwave = len(waves)
+        self._wave_plan = None
+        if self.nwave:
+            winst = (_Instance * self.nwave)(*[self._inst(i) for i in waves])
+            hb, db = ctypes.c_size_t(), ctypes.c_size_t()
+            nat.call("qf_wave_plan", ctypes.addressof(winst), self.nwave, self.layout, None, 0,
+                     ctypes.byref(hb), ctypes.byref(db))
+            plan = np.zeros(hb.value, dtype=np.uint8)
+            nat.call("qf_wave_plan", ctypes.addressof(winst), self.nwave, self.layout, plan.ctypes.data,
+                     hb.value, None, None)
+            self._wave_plan = plan
+            self.wave_ws_bytes = db.value
+            self.wave_ws = torch.empty(max(db.value, 256), dtype=torch.uint8, device=self.device)
+            nat.call("qf_wave_prepare", plan.ctypes.data, nat.ptr(self.d_edges), nat.ptr(self.wave_ws),
+                     self.wave_ws_bytes, nat.stream_handle(self.device))
         self._graph = None
+
+    def _inst(self, i):
+        return _Instance(int(self.ns[i]), int(self.ps[i]), int(self.nedges[i]), int(self.edge_offset[i]),
+                         int(self.angle_offset[i]), int(self.out_offset[i]))
 
     # ------------------------------------------------------------ angles ---
     def set_angles(self, betas, gammas):
@@ -138,9 +173,14 @@ class QAOABatch:
     # ------------------------------------------------------------ launch ---
     def launch(self, stream=None):
         """Enqueue one evaluation (asynchronous)."""
-        nat.call("qf_batch_qaoa_grad", nat.ptr(self.d_inst), self.count, self.nlarge, nat.ptr(self.d_edges),
-                 nat.ptr(self.angles), nat.ptr(self.out), self.layout, self.max_n, self.tile_bits,
-                 self.ctas, nat.ptr(self.ws), self.ws_bytes, stream or nat.stream_handle(self.device))
+        stream = stream or nat.stream_handle(self.device)
+        if self.nsmall:
+            nat.call("qf_batch_qaoa_grad", nat.ptr(self.d_inst), self.nsmall, self.nlarge, nat.ptr(self.d_edges),
+                     nat.ptr(self.angles), nat.ptr(self.out), self.layout, self.small_max_n, self.tile_bits,
+                     self.ctas, nat.ptr(self.ws), self.ws_bytes, stream)
+        if self.nwave:
+            nat.call("qf_wave_qaoa_grad", self._wave_plan.ctypes.data, nat.ptr(self.wave_ws), self.wave_ws_bytes,
+                     nat.ptr(self.angles), nat.ptr(self.out), stream)
 
     def expectations(self) -> torch.Tensor:
         """<C> per instance (device tensor, input order) from the last launch."""

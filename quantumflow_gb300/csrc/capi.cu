@@ -24,6 +24,12 @@ int batch_qaoa(const qf_batch_instance* inst, int ninst, int nlarge, const uint8
                cudaStream_t stream);
 int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
               const double* gamma, const double* node_theta, double* out, void* ws, cudaStream_t stream);
+int wave_min_qubits(int layout);
+int wave_plan(const qf_batch_instance* hinst, int ninst, int layout, void* host_plan, size_t host_bytes,
+              size_t* need_host, size_t* need_device);
+int wave_prepare(const void* host_plan, const uint8_t* edges, void* ws, size_t ws_bytes, cudaStream_t stream);
+int wave_run(const void* host_plan, void* ws, size_t ws_bytes, const double* angles, double* out,
+             cudaStream_t stream);
 }  // namespace qf
 
 using namespace qf;
@@ -220,6 +226,35 @@ int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges
   if (nedges + 1 > 1024) return QF_ERR_TOO_LARGE;
   return qaoa_state(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, fusion_k,
                     as_stream(stream));
+}
+
+int qf_wave_min_qubits(int layout) {
+  if (layout != QF_LAYOUT_C64 && layout != QF_LAYOUT_FF) return -QF_ERR_LAYOUT;
+  return wave_min_qubits(layout);
+}
+
+int qf_wave_plan(const qf_batch_instance* instances, int ninstances, int layout, void* host_plan,
+                 size_t host_bytes, size_t* host_bytes_needed, size_t* device_bytes_needed) {
+  if (ninstances < 0 || (ninstances > 0 && instances == nullptr)) return QF_ERR_INVALID_ARGUMENT;
+  if (host_plan == nullptr && host_bytes_needed == nullptr && device_bytes_needed == nullptr)
+    return QF_ERR_INVALID_ARGUMENT;
+  return wave_plan(instances, ninstances, layout, host_plan, host_bytes, host_bytes_needed, device_bytes_needed);
+}
+
+int qf_wave_prepare(const void* host_plan, const uint8_t* edges, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+  if (host_plan == nullptr || edges == nullptr) return QF_ERR_INVALID_ARGUMENT;
+  if (workspace == nullptr) return QF_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
+  return wave_prepare(host_plan, edges, workspace, workspace_bytes, as_stream(stream));
+}
+
+int qf_wave_qaoa_grad(const void* host_plan, void* workspace, size_t workspace_bytes, const double* angles,
+                      double* out, void* stream) {
+  if (host_plan == nullptr || angles == nullptr || out == nullptr) return QF_ERR_INVALID_ARGUMENT;
+  if (workspace == nullptr) return QF_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
+  return wave_run(host_plan, workspace, workspace_bytes, angles, out, as_stream(stream));
 }
 
 size_t qf_batch_workspace_bytes(int max_n, int layout, int ctas) {

@@ -46,14 +46,17 @@ def test_batch_matches_single_instance(dtype, tol):
 
 @pytest.mark.parametrize("tile_bits", [8, 9, 10])
 def test_batch_large_instances_tiled(tile_bits):
-    """Instances above the tile size run the global-scratch tiled passes."""
+    """With multi-instance passes held back, instances above the tile size
+    run the persistent kernel's global-scratch tiled passes (clusters of 8
+    CTAs from tile + 4 qubits)."""
     import quantumflow_gb300 as qf
     rng = np.random.default_rng(9)
     graphs = [qf.qaoa.random_regular_graph(3, n, seed=n) for n in (12, 14, 16, 10)]
     ps = [3, 2, 2, 4]
     betas = [rng.uniform(0, np.pi, p) for p in ps]
     gammas = [rng.uniform(0, np.pi, p) for p in ps]
-    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128", tile_bits=tile_bits, ctas=16)
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex128", tile_bits=tile_bits, ctas=16, wave_min=99)
+    assert batch.nwave == 0
     assert batch.nlarge == sum(n >= tile_bits + 4 for n in (12, 14, 16, 10))
     batch.set_angles(betas, gammas)
     es, dbs, dgs = batch.evaluate()
@@ -62,6 +65,55 @@ def test_batch_large_instances_tiled(tile_bits):
         assert abs(es[i] - e) < 1e-9
         np.testing.assert_allclose(dbs[i], gb, atol=1e-8)
         np.testing.assert_allclose(dgs[i], gg, atol=1e-8)
+
+
+@pytest.mark.parametrize("dtype,tol", [("complex64", 2e-4), ("complex128", 1e-9)])
+@pytest.mark.parametrize("tile_bits", [8, 10])
+def test_batch_wave_passes_match_single_instance(dtype, tol, tile_bits):
+    """Uneven instances above the tile size (n up to 18, p 1..5) as
+    multi-instance warp-tile passes, mixed with shared-memory instances in
+    one evaluation, against the single-instance adjoint path."""
+    import quantumflow_gb300 as qf
+    graphs, ps, rng = _mixed_instances(24, 17, nmin=6, nmax=18, pmax=5)
+    betas = [rng.uniform(0, np.pi, p) for p in ps]
+    gammas = [rng.uniform(0, np.pi, p) for p in ps]
+    batch = qf.batched.QAOABatch(graphs, ps, dtype=dtype, tile_bits=tile_bits, ctas=152)
+    assert batch.nwave == sum(g.number_of_nodes() > tile_bits for g in graphs)
+    assert 0 < batch.nwave < len(graphs)
+    batch.set_angles(betas, gammas)
+    es, dbs, dgs = batch.evaluate()
+    for i in range(len(graphs)):
+        e, gb, gg = qf.QAOAMaxCut(graphs[i], ps[i]).expectation_and_grad(betas[i], gammas[i])
+        scale = max(1.0, abs(e))
+        assert abs(es[i] - e) < tol * scale, (i, es[i], e)
+        np.testing.assert_allclose(dbs[i], gb, atol=tol * scale * 4)
+        np.testing.assert_allclose(dgs[i], gg, atol=tol * scale * 4)
+    # a second evaluation with other angles reuses the uploaded plan
+    batch.set_angles(gammas, betas)
+    es2, _, _ = batch.evaluate()
+    for i in (0, len(graphs) - 1):
+        e = qf.QAOAMaxCut(graphs[i], ps[i]).expectation(gammas[i], betas[i])
+        assert abs(es2[i] - e) < tol * max(1.0, abs(e))
+
+
+def test_batch_wave_graph_replay():
+    """Adam steps replayed from a CUDA graph over multi-instance passes equal
+    the eager steps (the coefficient tables follow the device angles)."""
+    import quantumflow_gb300 as qf
+    graphs, ps, rng = _mixed_instances(12, 23, nmin=13, nmax=17, pmax=3)
+    batch = qf.batched.QAOABatch(graphs, ps, dtype="complex64", tile_bits=10)
+    assert batch.nwave == len(graphs)
+    betas = [np.full(p, 0.3) for p in ps]
+    gammas = [np.full(p, 0.3) for p in ps]
+    batch.set_angles(betas, gammas)
+    e0, _, _ = batch.evaluate()
+    batch.adam(12, lr=0.05, use_graph=True)
+    e1, _, _ = batch.evaluate()
+    assert np.mean(e1 - e0) > 0.05
+    batch.set_angles(betas, gammas)
+    batch.adam(12, lr=0.05, use_graph=False)
+    e2, _, _ = batch.evaluate()
+    np.testing.assert_allclose(e2, e1, rtol=1e-5, atol=1e-5)
 
 
 def test_batch_reference_fixtures(golden):

@@ -65,3 +65,36 @@ def test_graph_generators():
     assert 60 < g2.number_of_edges() < 130
     with pytest.raises(ValueError):
         qf.qaoa.random_regular_graph(3, 7)
+
+
+def test_wave_plan_host_logic():
+    """The multi-instance pass planner runs on the host only: pass counts
+    1 + p (m - 1) per sweep (m register-bit groups), the output count, and
+    the rejection of instances it cannot run."""
+    import ctypes
+    from quantumflow_gb300 import _native as nat
+    from quantumflow_gb300.batched import _Instance
+    inst = (_Instance * 2)(_Instance(20, 6, 30, 0, 0, 0), _Instance(16, 3, 24, 30, 12, 13))
+    hb, db = ctypes.c_size_t(), ctypes.c_size_t()
+    assert nat.lib.qf_wave_plan(ctypes.addressof(inst), 2, nat.LAYOUT_C64, None, 0,
+                                ctypes.byref(hb), ctypes.byref(db)) == 0
+    plan = np.zeros(hb.value, np.uint8)
+    assert nat.lib.qf_wave_plan(ctypes.addressof(inst), 2, nat.LAYOUT_C64, plan.ctypes.data, hb.value,
+                                None, None) == 0
+    magic, layout, rbf, rba, ninst, nwaves, nfwd, nadj, nsegs, nout = plan[:40].view(np.int32)
+    assert (layout, rbf, rba, ninst) == (nat.LAYOUT_C64, 4, 3, 2)
+    # forward: n=20 -> 4 groups of <= 4 high bits: 1 + 6*3; n=16 -> 3 groups: 1 + 3*2
+    # adjoint: n=20 -> 5 groups of <= 3: 1 + 6*4; n=16 -> 4 groups: 1 + 3*3
+    assert nfwd == 19 + 7 and nadj == 25 + 10 and nwaves == max(19 + 25, 7 + 10)
+    assert nout == (2 * 6 + 1) + (2 * 3 + 1)
+    # the device workspace holds both states and the cut table of each instance
+    assert db.value > (2 * 8 + 2) * (2 ** 20 + 2 ** 16)
+    assert nat.lib.qf_wave_plan(ctypes.addressof(inst), 2, nat.LAYOUT_C64, plan.ctypes.data, 16,
+                                None, None) == 8
+    bad = (_Instance * 1)(_Instance(6, 2, 5, 0, 0, 0))  # below the warp tile
+    assert nat.lib.qf_wave_plan(ctypes.addressof(bad), 1, nat.LAYOUT_C64, None, 0,
+                                ctypes.byref(hb), ctypes.byref(db)) == 1
+    bad = (_Instance * 1)(_Instance(12, 0, 5, 0, 0, 0))  # p = 0
+    assert nat.lib.qf_wave_plan(ctypes.addressof(bad), 1, nat.LAYOUT_FF, None, 0,
+                                ctypes.byref(hb), ctypes.byref(db)) == 1
+    assert nat.lib.qf_wave_min_qubits(nat.LAYOUT_C64) == 9 and nat.lib.qf_wave_min_qubits(nat.LAYOUT_FF) == 8
