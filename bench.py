@@ -194,7 +194,37 @@ def qaoa_time_to_ratio(args):
     for _ in range(reps):
         prob24.expectation_and_grad(b24, g24a)
     grad_rate = reps / (time.perf_counter() - t0)
+    # batched evaluation of 4096 uneven instances (n 10..20, p 1..6; half
+    # G(n, 0.5), half random 3-regular where n is even): <C> and adjoint
+    # gradient of every instance per evaluation
+    c4 = {}
+    rng4 = np.random.default_rng(4096)
+    g4, p4 = [], []
+    for i in range(4096):
+        n = int(rng4.integers(10, 21))
+        if i % 2 and n % 2 == 0:
+            g4.append(qf.qaoa.random_regular_graph(3, n, seed=int(rng4.integers(1 << 30))))
+        else:
+            g4.append(qf.qaoa.gnp_random_graph(n, 0.5, seed=int(rng4.integers(1 << 30))))
+        p4.append(int(rng4.integers(1, 7)))
+    b4 = [rng4.uniform(0, np.pi, p) for p in p4]
+    gm4 = [rng4.uniform(0, np.pi, p) for p in p4]
+    for dt in ("complex64", "complex128"):
+        batch = qf.batched.QAOABatch(g4, p4, dtype=dt)
+        batch.set_angles(b4, gm4)
+        batch.launch()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            batch.launch()
+        e1.record()
+        torch.cuda.synchronize()
+        c4[dt] = e0.elapsed_time(e1) / 3
+        del batch
+        torch.cuda.empty_cache()
     return {"workload": f"{len(graphs)} random 3-regular graphs, n=20, p=6, target ratio 0.90, complex64",
+            "batched_4096_uneven_eval_ms": c4,
             "plain_init_single_s": plain_s, "plain_init_batched_s": res["plain_batched"]["seconds"],
             "learned_init_batched_s": learned_s, "speedup_learned_batched_vs_plain_single": plain_s / learned_s,
             "initial_ratio_plain": init_plain, "initial_ratio_learned": init_learned,

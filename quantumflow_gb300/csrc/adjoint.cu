@@ -385,14 +385,26 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
     // mixer: each bit's reduction precedes its own RX(-beta); the
     // reduction on bit j is unchanged by RX already undone on other bits
     // (same unitary on both vectors) and commutes with X_j
+    // complex64: a sub-tile's reduction terms are summed in FP32 and added
+    // to the compensated accumulator once
+    constexpr bool F32 = LAY == C64;
+    auto redx = [&](FFAcc& acc, float& part, const E& lv, const E& pv) {
+      if constexpr (F32) {
+        part = fmaf(lv.x, pv.y, part);
+        part = fmaf(-lv.y, pv.x, part);
+      } else {
+        redx_acc(acc, lv, pv);
+      }
+    };
     auto mixer = [&](const Coef& mc, const Coef& ms, bool lanes, int nact, FFAcc& acc) {
+      float part = 0.f;
       if (lanes) {
         for (int b = 0; b < 5; ++b) {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const E pa = shfl_xor(a[r], 1 << b);
             const E pl = shfl_xor(l[r], 1 << b);
-            redx_acc(acc, l[r], pa);
+            redx(acc, part, l[r], pa);
             a[r] = rx_one(mc, ms, a[r], pa);
             l[r] = rx_one(mc, ms, l[r], pl);
           }
@@ -405,8 +417,8 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
           for (int i = 0; i < R / 2; ++i) {
             const int i0 = ((i >> j) << (j + 1)) | (i & ((1 << j) - 1));
             const int i1 = i0 | (1 << j);
-            redx_acc(acc, l[i0], a[i1]);
-            redx_acc(acc, l[i1], a[i0]);
+            redx(acc, part, l[i0], a[i1]);
+            redx(acc, part, l[i1], a[i0]);
             const E a0 = a[i0], l0 = l[i0];
             a[i0] = rx_one(mc, ms, a0, a[i1]);
             a[i1] = rx_one(mc, ms, a[i1], a0);
@@ -415,14 +427,23 @@ __global__ void __launch_bounds__(256) k_adjw(const __grid_constant__ AdjWParams
           }
         }
       }
+      if constexpr (F32) acc.add(part, 0.f);
     };
     mixer(rc, rs, P.lanes != 0, P.nact, ax);
     if (P.last) {
       uint32_t cv[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) cv[r] = P.cuts[xb | hoff[r]];
+      if constexpr (F32) {
+        float part = 0.f;
 #pragma unroll
-      for (int r = 0; r < R; ++r) acc_imconj(ac, to_ff(l[r]), to_ff(a[r]), P.wref - (float)cv[r]);
+        for (int r = 0; r < R; ++r)
+          part = fmaf(P.wref - (float)cv[r], fmaf(l[r].x, a[r].y, -l[r].y * a[r].x), part);
+        ac.add(part, 0.f);
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc_imconj(ac, to_ff(l[r]), to_ff(a[r]), P.wref - (float)cv[r]);
+      }
       for (int d = 0; d < P.ndiag; ++d) {
         const int gb = P.diag_bit[d];
 #pragma unroll

@@ -345,25 +345,43 @@ __global__ void __launch_bounds__(256) k_wave_adj(const WvAdj* items, int nitems
     uint32_t cv[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) cv[r] = gc[xb | hoff[r]];
+    // complex64: each thread sums one sub-tile's terms of a reduction in
+    // FP32 and adds that partial to the compensated accumulator once
+    constexpr bool F32 = LAY == C64;
     if (A.init) {
+      float part = 0.f;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const float c = (float)cv[r];
-        FFAcc t;
-        t.zero();
-        acc_norm2(t, a[r]);
-        ae.add_prod(c, 0.f, t.s, t.e);
+        if constexpr (F32) {
+          part = fmaf(c, fmaf(a[r].x, a[r].x, a[r].y * a[r].y), part);
+        } else {
+          FFAcc t;
+          t.zero();
+          acc_norm2(t, a[r]);
+          ae.add_prod(c, 0.f, t.s, t.e);
+        }
         l[r] = scale_ff(a[r], c);
       }
+      if constexpr (F32) ae.add(part, 0.f);
     }
+    auto redx = [&](FFAcc& acc, float& part, const E& lv, const E& pv) {
+      if constexpr (F32) {
+        part = fmaf(lv.x, pv.y, part);
+        part = fmaf(-lv.y, pv.x, part);
+      } else {
+        redx_acc(acc, lv, pv);
+      }
+    };
     auto mixer = [&](const Coef& c0, const Coef& s0, bool lanes, int nact, FFAcc& acc) {
+      float part = 0.f;
       if (lanes) {
         for (int b = 0; b < 5; ++b) {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const E pa = shfl_xor(a[r], 1 << b);
             const E pl = shfl_xor(l[r], 1 << b);
-            redx_acc(acc, l[r], pa);
+            redx(acc, part, l[r], pa);
             a[r] = rx_one(c0, s0, a[r], pa);
             l[r] = rx_one(c0, s0, l[r], pl);
           }
@@ -376,8 +394,8 @@ __global__ void __launch_bounds__(256) k_wave_adj(const WvAdj* items, int nitems
           for (int i = 0; i < R / 2; ++i) {
             const int i0 = ((i >> j) << (j + 1)) | (i & ((1 << j) - 1));
             const int i1 = i0 | (1 << j);
-            redx_acc(acc, l[i0], a[i1]);
-            redx_acc(acc, l[i1], a[i0]);
+            redx(acc, part, l[i0], a[i1]);
+            redx(acc, part, l[i1], a[i0]);
             const E a0 = a[i0], l0 = l[i0];
             a[i0] = rx_one(c0, s0, a0, a[i1]);
             a[i1] = rx_one(c0, s0, a[i1], a0);
@@ -386,11 +404,20 @@ __global__ void __launch_bounds__(256) k_wave_adj(const WvAdj* items, int nitems
           }
         }
       }
+      if constexpr (F32) acc.add(part, 0.f);
     };
     mixer(mc, ms, A.lanes != 0, A.nact, ax);
     if (A.last) {
+      if constexpr (F32) {
+        float part = 0.f;
 #pragma unroll
-      for (int r = 0; r < R; ++r) acc_imconj(acu, to_ff(l[r]), to_ff(a[r]), wref - (float)cv[r]);
+        for (int r = 0; r < R; ++r)
+          part = fmaf(wref - (float)cv[r], fmaf(l[r].x, a[r].y, -l[r].y * a[r].x), part);
+        acu.add(part, 0.f);
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc_imconj(acu, to_ff(l[r]), to_ff(a[r]), wref - (float)cv[r]);
+      }
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const Coef& c = scut[min((int)cv[r], E1 - 1)];
