@@ -179,6 +179,36 @@ def program_ops(names, params, qubits):
     return ops
 
 
+# ------------------------------------------------------ density matrices --
+def gate_superop(u):
+    """Superoperator of a k-qubit gate as a (4^k, 4^k) matrix, rows (ket-out,
+    bra-out), columns (ket-in, bra-in): outer(U, U^dagger) with index groups
+    (0, 3, 1, 2) (quantumflow/ops.py:244-253)."""
+    u = np.asarray(u, dtype=np.complex128)
+    d = u.shape[0]
+    t = np.multiply.outer(u, np.conj(u).T).reshape(d, d, d, d).transpose(0, 3, 1, 2)
+    return t.reshape(d * d, d * d)
+
+
+def kraus_superop(ops, weights=None):
+    """sum_k w_k superop(K_k) for operators on the same qubits
+    (quantumflow/channels.py:58-68)."""
+    weights = [1.0] * len(ops) if weights is None else weights
+    return sum(w * gate_superop(k) for k, w in zip(ops, weights))
+
+
+def evolve_density(rho, superop, axes):
+    """rho (2^N x 2^N) after a channel on qubit axes `axes`: the superoperator
+    contracted with the ket and bra axes of rho as a 2N-index tensor
+    (quantumflow/ops.py:354-363, tensormul of numpybk.py:159-214)."""
+    rho = np.asarray(rho, dtype=np.complex128)
+    M = rho.shape[0]
+    N = int(round(np.log2(M)))
+    t = rho.reshape([2] * (2 * N))
+    out = tensormul(np.asarray(superop).reshape([2] * (4 * len(axes))), t, list(axes) + [N + a for a in axes])
+    return out.reshape(M, M)
+
+
 # ------------------------------------------------------------- QAOA --------
 def qubo_ops(n, edges, p, beta, gamma, weights=None, node_weights=None):
     """Gate list of quantumflow/qaoa.py:22-64 qubo_circuit for nodes 0..n-1:

@@ -16,6 +16,8 @@ from .gates import *  # noqa: F401,F403
 from .stdgates import *  # noqa: F401,F403
 from .circuits import *  # noqa: F401,F403
 from .measures import *  # noqa: F401,F403
+from .densities import *  # noqa: F401,F403
+from .channels import *  # noqa: F401,F403
 from .cbits import *  # noqa: F401,F403
 from .stdops import *  # noqa: F401,F403
 from .programs import *  # noqa: F401,F403

@@ -118,6 +118,32 @@ class Circuit(Operation):
         self.last_passes = passes[0]
         return State(out, ket.qubits, ket._memory)
 
+    def evolve(self, rho=None):
+        """Apply the circuit to a density matrix (quantumflow/circuits.py
+        Circuit.evolve); each run of consecutive gates is one fused launch on
+        the density's ket and bra axes.  Default: |0...0><0...0|."""
+        from .densities import evolve_gates
+        if rho is None:
+            rho = zero_state(self.qubits).asdensity()
+        pending = []
+        for elem in self.gates():
+            if isinstance(elem, Gate):
+                pending.append(elem)
+                continue
+            if pending:
+                rho = evolve_gates(rho, pending)
+                pending = []
+            rho = elem.evolve(rho)
+        return evolve_gates(rho, pending) if pending else rho
+
+    def aschannel(self):
+        """Composite superoperator of the elements, in order."""
+        from .channels import gate_aschannel
+        out = gate_aschannel(identity_gate(self.qubits))
+        for elem in self.elements:
+            out = elem.aschannel() @ out
+        return out
+
     def asgate(self) -> Gate:
         gate = identity_gate(self.qubits)
         for elem in self.elements:

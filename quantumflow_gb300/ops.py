@@ -38,7 +38,14 @@ class Operation(ABC):
     def run(self, ket: State) -> State:
         raise NotImplementedError()
 
+    def evolve(self, rho):
+        """Apply this operation to a density matrix (quantumflow/ops.py:62-64)."""
+        raise NotImplementedError()
+
     def asgate(self) -> "Gate":
+        raise NotImplementedError()
+
+    def aschannel(self):
         raise NotImplementedError()
 
     @property
@@ -142,6 +149,17 @@ class Gate(Operation):
 
     def asgate(self) -> "Gate":
         return self
+
+    def evolve(self, rho):
+        """Apply to a density matrix (quantumflow/ops.py:168-172): U on the
+        ket axes and conj(U) on the bra axes, one fused launch."""
+        from .densities import evolve_gates
+        return evolve_gates(rho, [self])
+
+    def aschannel(self):
+        """The gate's superoperator (quantumflow/ops.py:244-253)."""
+        from .channels import gate_aschannel
+        return gate_aschannel(self)
 
     def su(self) -> "Gate":
         rank = 2 ** self.qubit_nb

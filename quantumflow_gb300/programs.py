@@ -64,7 +64,9 @@ class Instruction(ABC):
         raise NotImplementedError()
 
     def evolve(self, rho):
-        raise TypeError("density-matrix evolution is not part of this backend")
+        """Classical and control instructions act alike on densities
+        (quantumflow/programs.py:82-87)."""
+        return self.run(rho)
 
 
 def _is_gate_instruction(instr) -> bool:
@@ -136,6 +138,31 @@ class Program(Instruction):
                 ket = instr.run(ket)
             pc = ket.memory[PC]
         return ket
+
+    def evolve(self, rho=None):
+        """Run the program on a density matrix (quantumflow/programs.py:175-191);
+        runs of gate instructions are fused as in :meth:`run`."""
+        from .densities import evolve_gates
+        if rho is None:
+            rho = zero_state(self.qubits).asdensity()
+        rho = self._initilize(rho)
+        pc = 0
+        while 0 <= pc < len(self):
+            instr = self.instructions[pc]
+            if _is_gate_instruction(instr):
+                end = self._gate_run_end(pc)
+                namedgates = rho.memory[NAMEDGATES]
+                gates = []
+                for g in self.instructions[pc:end]:
+                    gates.extend(g.gates() if isinstance(g, Circuit) else
+                                 [g.asgate_from(namedgates) if isinstance(g, Call) else g])
+                rho = rho.update({PC: end})
+                rho = Circuit(gates).evolve(rho)
+            else:
+                rho = rho.update({PC: pc + 1})
+                rho = instr.evolve(rho)
+            pc = rho.memory[PC]
+        return rho
 
 
 class DefCircuit(Program):
@@ -330,6 +357,9 @@ class Call(Instruction):
 
     def run(self, ket: State) -> State:
         return self.asgate_from(ket.memory[NAMEDGATES]).run(ket)
+
+    def evolve(self, rho):
+        return self.asgate_from(rho.memory[NAMEDGATES]).evolve(rho)
 
 
 class Declare(Instruction):

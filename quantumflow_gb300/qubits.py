@@ -89,6 +89,33 @@ class QubitVector:
     def norm(self) -> float:
         return float(np.abs(np.vdot(self.tensor, self.tensor)))
 
+    def trace(self) -> complex:
+        """Sum of the diagonal of the (super)operator (quantumflow/qubits.py:185-197)."""
+        if self.rank == 1:
+            raise ValueError("Cannot take trace of vector")
+        N, R = self.qubit_nb, self.rank
+        return complex(np.trace(self.tensor.reshape([2 ** (N * R // 2)] * 2)))
+
+    def partial_trace(self, qubits: Qubits) -> "QubitVector":
+        """Trace over some of the qubits (quantumflow/qubits.py:201-225): the
+        remaining qubits keep their order."""
+        if self.rank == 1:
+            raise ValueError("Cannot take trace of vector")
+        N, R = self.qubit_nb, self.rank
+        keep = [q for q in self.qubits if q not in set(qubits)]
+        if not keep:
+            raise ValueError("Cannot remove all qubits with partial_trace.")
+        t = self.tensor
+        # contract each traced qubit's index in every rank group with the first
+        idx = [self.qubits.index(q) for q in qubits]
+        letters = [chr(ord("a") + i) if i < 26 else chr(ord("A") + i - 26) for i in range(N * R)]
+        for i in idx:
+            for r in range(1, R):
+                letters[r * N + i] = letters[i]
+        out = [letters[r * N + self.qubits.index(q)] for r in range(R) for q in keep]
+        res = np.einsum("".join(letters) + "->" + "".join(out), t)
+        return QubitVector(res, tuple(keep), R)
+
 
 def inner_product(vec0, vec1):
     """Hilbert-Schmidt inner product (quantumflow/qubits.py:227-238)."""

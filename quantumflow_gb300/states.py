@@ -178,6 +178,11 @@ class State:
     def asarray(self) -> np.ndarray:
         return self.tensor.detach().cpu().numpy()
 
+    def asdensity(self):
+        """|psi><psi| as a Density (quantumflow/states.py:162-165)."""
+        from .densities import asdensity
+        return asdensity(self)
+
     def norm(self) -> float:
         """|<psi|psi>| (quantumflow/qubits.py:180-182)."""
         return abs(_reduce("qf_norm2", self._buf, nout=1)[0])

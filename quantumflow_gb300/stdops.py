@@ -62,6 +62,21 @@ class Measure(Operation):
             ket = ket.update({self.cbit: outcome})
         return ket
 
+    def evolve(self, rho):
+        """Projective measurement of a density matrix, as the reference does
+        it (quantumflow/stdops.py:66-82): the outcome-0 weight it rolls
+        against is the norm (sum |rho'_ij|^2) of the projected density
+        rho' = P0 rho P0, and the kept branch is renormalised by its trace."""
+        from .gates import P0, P1
+        r0 = P0(self.qubit).evolve(rho)
+        if np.random.random() < r0.norm():
+            rho, outcome = r0.normalize(), 0
+        else:
+            rho, outcome = P1(self.qubit).evolve(rho).normalize(), 1
+        if self.cbit is not None:
+            rho = rho.update({self.cbit: outcome})
+        return rho
+
 
 class Reset(Operation):
     """Reset qubits (all of the state's qubits if none are given) to |0>,
@@ -85,8 +100,14 @@ class Reset(Operation):
         circ = Circuit([Gate(self._MAP, qubits=[q]) for q in qubits])
         return circ.run(ket).normalize()
 
+    def evolve(self, rho):
+        raise TypeError("Not yet implemented")  # as the reference (quantumflow/stdops.py:114-116)
+
     def asgate(self) -> Gate:
         raise TypeError("Reset not convertible to Gate")
+
+    def aschannel(self):
+        raise TypeError("Reset not convertible to Channel")
 
     def quil(self) -> str:
         if self.qubits:
@@ -112,6 +133,9 @@ class Barrier(Operation):
     def run(self, ket: State) -> State:
         return ket
 
+    def evolve(self, rho):
+        return rho
+
     def quil(self) -> str:
         return self.name.upper() + " " + " ".join(str(q) for q in self.qubits)
 
@@ -134,9 +158,21 @@ class If(Operation):
             ket = self.element.run(ket)
         return ket
 
+    def evolve(self, rho):
+        if rho.memory[self.condition] == self.value:
+            rho = self.element.evolve(rho)
+        return rho
+
 
 # ----------------------------------------------------- classical operations --
-class Neg(Operation):
+class _Classical(Operation):
+    """Classical memory operations act alike on states and densities."""
+
+    def evolve(self, rho):
+        return self.run(rho)
+
+
+class Neg(_Classical):
     """Negate a value in classical memory."""
 
     def __init__(self, target: Addr) -> None:
@@ -150,7 +186,7 @@ class Neg(Operation):
         return f"{self.name.upper()} {self.target}"
 
 
-class Not(Operation):
+class Not(_Classical):
     """Logical NOT of a classical bit."""
 
     def __init__(self, target: Addr) -> None:
@@ -163,7 +199,7 @@ class Not(Operation):
         return f"{self.name.upper()} {self.target}"
 
 
-class BinaryOP(Operation):
+class BinaryOP(_Classical):
     """target <- op(target, source); source is an address or a number."""
     _op: Callable = None
 
@@ -236,7 +272,7 @@ class Exchange(BinaryOP):
         return ket.update({self.target: ket.memory[self.source], self.source: ket.memory[self.target]})
 
 
-class Comparison(Operation):
+class Comparison(_Classical):
     """target <- op(memory[left], memory[right])."""
     _op: Callable = None
 

@@ -21,4 +21,4 @@ def load_golden(name):
 
 @pytest.fixture(scope="session")
 def golden():
-    return {n: load_golden(n + ".npz") for n in ("kat", "gates", "tensormul", "circuits", "qaoa", "programs")}
+    return {n: load_golden(n + ".npz") for n in ("kat", "gates", "tensormul", "circuits", "qaoa", "programs", "channels")}

@@ -404,6 +404,46 @@ def program_fixtures(qf, rng):
     return out
 
 
+# --------------------------------------------------------------- channels ----
+def channel_fixtures(qf, rng):
+    """Density-matrix evolution by the reference (quantumflow/ops.py:166-170
+    Gate.evolve via aschannel, :354-363 Channel.evolve, channels.py Kraus /
+    Damping / Depolarizing / Dephasing, states.py Density)."""
+    import scipy.stats
+    out = {}
+    N = 4
+    np.random.seed(20181205)
+    rho = qf.random_density(N)
+    out["rho0"] = np.asarray(rho.tensor).reshape(2 ** N, 2 ** N)
+    u1 = scipy.stats.unitary_group.rvs(2, random_state=rng)
+    u2 = scipy.stats.unitary_group.rvs(4, random_state=rng)
+    out["u1"], out["u2"] = u1, u2
+    steps = [
+        ("gate1", qf.Gate(u1, qubits=[2])),
+        ("gate2", qf.Gate(u2, qubits=[3, 0])),
+        ("damping", qf.Damping(0.3, 1)),
+        ("depolarizing", qf.Depolarizing(0.2, 3)),
+        ("dephasing", qf.Dephasing(0.45, 0)),
+        ("kraus2", qf.Kraus([qf.Gate(u2 * np.sqrt(0.7), qubits=[1, 2]),
+                             qf.Gate(np.eye(4) * np.sqrt(0.3), qubits=[1, 2])])),
+        ("chan_matmul", qf.Damping(0.1, 2).aschannel() @ qf.Dephasing(0.2, 2).aschannel()),
+        ("joined", qf.join_channels(qf.Damping(0.25, 0).aschannel(), qf.Depolarizing(0.15, 3).aschannel())),
+    ]
+    cur = rho
+    for name, op in steps:
+        cur = op.evolve(cur)
+        out[f"after_{name}"] = np.asarray(cur.tensor).reshape(2 ** N, 2 ** N)
+    out["trace_final"] = np.array(complex(qf.asarray(cur.trace())))
+    out["probs_final"] = np.asarray(cur.probabilities()).reshape(-1)
+    out["ptrace_13"] = np.asarray(cur.partial_trace([1, 3]).tensor).reshape(4, 4)
+    ket = qf.random_state(3)
+    out["ket"] = np.asarray(ket.tensor).reshape(-1)
+    out["ket_density"] = np.asarray(ket.asdensity().tensor).reshape(8, 8)
+    out["damping_superop"] = np.asarray(qf.Damping(0.3, 0).aschannel().tensor).reshape(4, 4)
+    out["mixed3"] = np.asarray(qf.mixed_density(3).tensor).reshape(8, 8)
+    return out
+
+
 def main():
     qf = import_reference()
     rng = np.random.default_rng(20181203)
@@ -414,6 +454,7 @@ def main():
         "circuits.npz": lambda: circuit_fixtures(qf, rng),
         "qaoa.npz": lambda: qaoa_fixtures(qf, rng),
         "programs.npz": lambda: program_fixtures(qf, np.random.default_rng(20181204)),
+        "channels.npz": lambda: channel_fixtures(qf, np.random.default_rng(20181205)),
     }
     only = set(sys.argv[1:])  # e.g. `programs` to rewrite programs.npz alone
     for fname, arrays in files.items():

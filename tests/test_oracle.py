@@ -95,3 +95,41 @@ def test_oracle_matches_reference_programs(golden):
         st = orc.run_ops(orc.zero_state(nq), ops).reshape(-1)
         assert np.max(np.abs(st - g[f"p{case}_state"])) < 1e-12
     np.testing.assert_allclose(g["wf_true"], golden["kat"]["true_ket"], atol=1e-12)
+
+
+def _channel_steps(c):
+    """(superop, axes) of each fixture step, built from the published channel
+    definitions (quantumflow/channels.py:128-166)."""
+    I2, X, Y, Z = np.eye(2), orc.X(), np.array([[0, -1j], [1j, 0]]), np.diag([1.0, -1.0])
+    def damp(p):
+        return orc.kraus_superop([np.array([[1, 0], [0, np.sqrt(1 - p)]]), np.array([[0, np.sqrt(p)], [0, 0]])])
+    def depol(p):
+        return orc.kraus_superop([I2, X, Y, Z], [1 - p, p / 3, p / 3, p / 3])
+    def deph(p):
+        return orc.kraus_superop([I2, Z], [1 - p / 2, p / 2])
+    u1, u2 = c["u1"], c["u2"]
+    # Gate(u2, qubits=[3, 0]): matrix MSB on qubit 3
+    return [
+        ("gate1", orc.gate_superop(u1), [2]),
+        ("gate2", orc.gate_superop(u2), [3, 0]),
+        ("damping", damp(0.3), [1]),
+        ("depolarizing", depol(0.2), [3]),
+        ("dephasing", deph(0.45), [0]),
+        ("kraus2", orc.kraus_superop([u2 * np.sqrt(0.7), np.eye(4) * np.sqrt(0.3)]), [1, 2]),
+        ("chan_matmul", damp(0.1) @ deph(0.2), [2]),
+    ]
+
+
+def test_oracle_matches_reference_channels(golden):
+    """Density evolution by superoperators in the oracle reproduces the
+    reference's Gate.evolve / Kraus channels / channel composition."""
+    c = golden["channels"]
+    rho = c["rho0"]
+    for name, sop, axes in _channel_steps(c):
+        rho = orc.evolve_density(rho, sop, axes)
+        assert np.max(np.abs(rho - c[f"after_{name}"])) < 1e-12, name
+    np.testing.assert_allclose(orc.kraus_superop([np.array([[1, 0], [0, np.sqrt(0.7)]]),
+                                                  np.array([[0, np.sqrt(0.3)], [0, 0]])]),
+                               c["damping_superop"], atol=1e-15)
+    ket = c["ket"]
+    np.testing.assert_allclose(np.outer(ket, ket.conj()), c["ket_density"], atol=1e-15)
