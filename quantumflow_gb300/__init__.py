@@ -18,9 +18,10 @@ from .circuits import *  # noqa: F401,F403
 from .measures import *  # noqa: F401,F403
 from .densities import *  # noqa: F401,F403
 from .channels import *  # noqa: F401,F403
+from .dagcircuit import *  # noqa: F401,F403
 from .cbits import *  # noqa: F401,F403
 from .stdops import *  # noqa: F401,F403
 from .programs import *  # noqa: F401,F403
 from .qaoa import qubo_circuit, graph_cuts, QAOAMaxCut, QAOAExpectation, Graph, maxcut_qaoa  # noqa: F401
 from . import qaoa  # noqa: F401
-from . import batched, autotune, gnn, adjoint  # noqa: F401
+from . import batched, autotune, gnn, adjoint, datasets  # noqa: F401

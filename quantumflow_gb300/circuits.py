@@ -16,7 +16,8 @@ from .ops import Gate, Operation
 from .qubits import Qubits
 from .states import Buffer, State, compute_layout, zero_state
 
-__all__ = ["Circuit", "count_operations"]
+__all__ = ["Circuit", "count_operations", "map_gate", "reversal_circuit", "qft_circuit", "control_circuit",
+           "ccnot_circuit", "zyz_circuit", "phase_estimation_circuit", "addition_circuit", "ghz_circuit"]
 
 
 class Circuit(Operation):
@@ -165,3 +166,120 @@ def count_operations(elements) -> dict:
     for e in elements:
         out[type(e)] = out.get(type(e), 0) + 1
     return out
+
+
+# ------------------------------------------------------- circuit library ----
+# The constructions below follow the reference gate for gate
+# (quantumflow/circuits.py:152-372), so that their states match it.
+def map_gate(gate: Gate, args) -> Circuit:
+    """The same gate on each qubit list of ``args`` (quantumflow/circuits.py:152-167)."""
+    return Circuit([gate.relabel(qubits) for qubits in args])
+
+
+def reversal_circuit(qubits) -> Circuit:
+    """SWAPs that reverse the qubit order (quantumflow/circuits.py:187-193)."""
+    from .stdgates import SWAP
+    N = len(qubits)
+    return Circuit([SWAP(qubits[n], qubits[N - 1 - n]) for n in range(N // 2)])
+
+
+def qft_circuit(qubits) -> Circuit:
+    """Quantum Fourier transform: H and CPHASE(pi / 2^d) ladders, then the
+    qubit reversal (quantumflow/circuits.py:170-184)."""
+    from math import pi
+    from .stdgates import CPHASE, H
+    qubits = list(qubits)
+    N = len(qubits)
+    circ = Circuit()
+    for n0 in range(N):
+        circ += H(qubits[n0])
+        for n1 in range(n0 + 1, N):
+            circ += CPHASE(pi / 2 ** (n1 - n0), qubits[n1], qubits[n0])
+    circ.extend(reversal_circuit(qubits))
+    return circ
+
+
+def control_circuit(controls, gate: Gate) -> Circuit:
+    """A gate controlled by several qubits, Barenco et al. 1995 sec. 7.2
+    (quantumflow/circuits.py:196-224)."""
+    from .gates import control_gate
+    from .stdgates import CNOT, X
+    circ = Circuit()
+    if len(controls) == 1:
+        q0 = controls[0]
+        circ += CNOT(q0, gate.qubits[0]) if isinstance(gate, X) else control_gate(q0, gate)
+    else:
+        circ += control_circuit(controls[-1:], gate ** 0.5)
+        circ += control_circuit(controls[0:-1], X(controls[-1]))
+        circ += control_circuit(controls[-1:], gate ** -0.5)
+        circ += control_circuit(controls[0:-1], X(controls[-1]))
+        circ += control_circuit(controls[0:-1], gate ** 0.5)
+    return circ
+
+
+def ccnot_circuit(qubits) -> Circuit:
+    """Toffoli as six CNOTs with H and T gates, Nielsen & Chuang
+    (quantumflow/circuits.py:227-257)."""
+    from .stdgates import CNOT, H, T
+    if len(qubits) != 3:
+        raise ValueError("Expected 3 qubits")
+    q0, q1, q2 = qubits
+    return Circuit([H(q2), CNOT(q1, q2), T(q2).H, CNOT(q0, q2), T(q2), CNOT(q1, q2), T(q2).H, CNOT(q0, q2),
+                    T(q1), T(q2), H(q2), CNOT(q0, q1), T(q0), T(q1).H, CNOT(q0, q1)])
+
+
+def zyz_circuit(t0: float, t1: float, t2: float, q0) -> Circuit:
+    """TZ TY TZ (quantumflow/circuits.py:260-266)."""
+    from .stdgates import TY, TZ
+    return Circuit([TZ(t0, q0), TY(t1, q0), TZ(t2, q0)])
+
+
+def phase_estimation_circuit(gate: Gate, outputs) -> Circuit:
+    """Quantum phase estimation (quantumflow/circuits.py:269-303)."""
+    from .gates import control_gate
+    from .stdgates import H
+    outputs = list(outputs)
+    circ = Circuit()
+    circ += map_gate(H(), list(zip(outputs)))
+    for cq in reversed(outputs):
+        circ += control_gate(cq, gate)
+        gate = gate @ gate
+    circ += qft_circuit(outputs).H
+    return circ
+
+
+def addition_circuit(addend0, addend1, carry) -> Circuit:
+    """Ripple-carry adder, Cuccaro et al. 2004 (quantumflow/circuits.py:306-356);
+    the sum replaces addend1."""
+    from itertools import chain
+    from .stdgates import CCNOT, CNOT
+    if len(addend0) != len(addend1):
+        raise ValueError("Number of addend qubits must be equal")
+    if len(carry) != 2:
+        raise ValueError("Expected 2 carry qubits")
+
+    def maj(q0, q1, q2):
+        return Circuit([CNOT(q2, q1), CNOT(q2, q0), CCNOT(q0, q1, q2)])
+
+    def uma(q0, q1, q2):
+        return Circuit([CCNOT(q0, q1, q2), CNOT(q2, q0), CNOT(q0, q1)])
+
+    qubits = [carry[0]] + list(chain.from_iterable(zip(reversed(list(addend1)), reversed(list(addend0))))) \
+        + [carry[1]]
+    circ = Circuit()
+    for n in range(0, len(qubits) - 3, 2):
+        circ += maj(*qubits[n:n + 3])
+    circ += CNOT(qubits[-2], qubits[-1])
+    for n in reversed(range(0, len(qubits) - 3, 2)):
+        circ += uma(*qubits[n:n + 3])
+    return circ
+
+
+def ghz_circuit(qubits) -> Circuit:
+    """H then a CNOT chain (quantumflow/circuits.py:359-370)."""
+    from .stdgates import CNOT, H
+    qubits = list(qubits)
+    circ = Circuit([H(qubits[0])])
+    for i in range(len(qubits) - 1):
+        circ += CNOT(qubits[i], qubits[i + 1])
+    return circ

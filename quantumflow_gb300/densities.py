@@ -147,7 +147,7 @@ def evolve_superop(rho: Density, superop: np.ndarray, qubits: Qubits) -> Density
     bra-out bits, columns ket-in then bra-in) as one 2k-qubit gate."""
     k = len(qubits)
     if 2 * k > 5:
-        raise ValueError("channels on more than two qubits are not supported on the GPU engine")
+        return _evolve_by_choi(rho, superop, qubits)
     N = rho.qubit_nb
     idx = [rho.qubits.index(q) for q in qubits]
     axes = idx + [N + i for i in idx]
@@ -158,6 +158,33 @@ def evolve_superop(rho: Density, superop: np.ndarray, qubits: Qubits) -> Density
              nat.int_array(axes), m.view(np.float64).reshape(-1).ctypes.data_as(nat._dp),
              nat.stream_handle(src.device))
     return Density(out, rho.qubits, rho._memory)
+
+
+def _evolve_by_choi(rho: Density, superop: np.ndarray, qubits: Qubits) -> Density:
+    """Channels on three or more qubits (whose 2k-qubit superoperator is above
+    the engine's 5-qubit dense gates): the Choi matrix's eigen-decomposition
+    gives sum_i l_i K_i (.) K_i^dagger (K_i = the i-th eigenvector as a
+    2^k x 2^k matrix, the reshaping of quantumflow/channels.py:181-203), and
+    every term is one k-qubit gate pair on the density's ket and bra axes."""
+    from .ops import Gate
+    k = len(qubits)
+    d = 2 ** k
+    choi = np.asarray(superop).reshape([d] * 4).transpose(0, 2, 1, 3).reshape(d * d, d * d)
+    if not np.allclose(choi, choi.conj().T, atol=1e-10):
+        raise ValueError("channel does not preserve Hermiticity")
+    evals, evecs = np.linalg.eigh(choi)
+    acc = None
+    for lam, vec in zip(evals, evecs.T):
+        if abs(lam) < 1e-14:
+            continue
+        term = evolve_gates(rho, [Gate(vec.reshape(d, d), qubits=qubits)])
+        t = term.buffer.complex().to(torch.complex128) * float(lam)
+        acc = t if acc is None else acc + t
+    if acc is None:
+        acc = torch.zeros(2 ** rho.buffer.n, dtype=torch.complex128, device=rho.buffer.device)
+    out = Density(acc.reshape([2] * rho.buffer.n), rho.qubits, rho._memory)
+    return out if rho.dtype == "complex128" else Density(acc.to(torch.complex64).reshape([2] * rho.buffer.n),
+                                                         rho.qubits, rho._memory)
 
 
 # ----------------------------------------------------------- constructors --

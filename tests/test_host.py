@@ -98,3 +98,44 @@ def test_wave_plan_host_logic():
     assert nat.lib.qf_wave_plan(ctypes.addressof(bad), 1, nat.LAYOUT_FF, None, 0,
                                 ctypes.byref(hb), ctypes.byref(db)) == 1
     assert nat.lib.qf_wave_min_qubits(nat.LAYOUT_C64) == 9 and nat.lib.qf_wave_min_qubits(nat.LAYOUT_FF) == 8
+
+
+def test_graph6_round_trip_and_networkx_agreement():
+    """graph6 encoding (size prefixes up to 258047 nodes, upper-triangle bits
+    column by column) round-trips, and matches networkx's encoder."""
+    from quantumflow_gb300 import datasets
+    graphs = [qf.qaoa.gnp_random_graph(n, 0.5, seed=n) for n in (1, 2, 6, 13, 32, 63, 70)]
+    text = datasets.write_graph6(graphs)
+    back = datasets.read_graph6(text)
+    assert len(back) == len(graphs)
+    for g, h in zip(graphs, back):
+        assert len(h) == len(g)
+        assert {tuple(sorted(e)) for e in g.edges()} == {tuple(sorted(e)) for e in h.edges()}
+    one = datasets.read_graph6(datasets.write_graph6(graphs[2:3], header=True))
+    assert len(one) == 6
+    nx = pytest.importorskip("networkx")
+    for g in graphs:
+        G = nx.Graph()
+        G.add_nodes_from(range(len(g)))
+        G.add_edges_from(g.edges())
+        assert nx.to_graph6_bytes(G, header=False).strip() == datasets.graph_to_graph6(g)
+    assert len(datasets.load_stdgraphs(12)) == 100
+    with pytest.raises(ValueError):
+        datasets.load_stdgraphs(5)
+
+
+def test_graph6_reads_reference_datasets():
+    """The reference's own graph sets (quantumflow/datasets/data/*.g6) read
+    the same as networkx reads them (runs where the reference is present)."""
+    import os
+    from quantumflow_gb300 import datasets
+    data = os.path.join(os.environ.get("QF_REFERENCE", "/root/reference"), "quantumflow", "datasets", "data")
+    if not os.path.isdir(data):
+        pytest.skip("reference datasets not present")
+    nx = pytest.importorskip("networkx")
+    for size in (6, 17, 32):
+        ours = datasets.load_stdgraphs(size, path=data)
+        theirs = nx.read_graph6(os.path.join(data, f"graph{size}er100.g6"))
+        assert len(ours) == len(theirs) == 100
+        for g, G in zip(ours, theirs):
+            assert {tuple(sorted(e)) for e in g.edges()} == {tuple(sorted(e)) for e in G.edges()}
