@@ -234,6 +234,17 @@ def qaoa_time_to_ratio(args):
             "adjoint_grad_evals_per_s_n24_p8_c128": grad_rate}
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's step time, on every rank (replicas: the whole job
+    is done when the last replica is)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank, world):
     """Reference arm: the CPU oracle port (the reference is pure Python; its
     numpy backend's tensormul is np.einsum, restated in oracle/qf_oracle.py)."""
@@ -358,11 +369,7 @@ def main():
     clock_info = clocks.stop()
     nat.timing_enable(False)
     kt = nat.timing_collect()
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, "cuda")
     value = world * ngates * sweep_bytes / (ms * 1e-3) / 1e9
     launches = sum(c for _, c in kt.values()) + args.steps  # + one |0> fill per step
 
