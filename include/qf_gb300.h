@@ -93,6 +93,14 @@ int qf_set_tile_kernel(int mode);
  * multiplied into blocks of at most two qubits on the host whenever
  * fusion_k > 1; 0 = every gate is applied as given. */
 int qf_set_gate_merging(int on);
+/* The pass plan qf_run_circuit would execute, without touching the GPU
+ * (diagnostics; no reference counterpart).  For each planned pass, 8 ints
+ * in stats[8*b ..]: ops, dense 1-qubit, dense 2-qubit, of those with a lane
+ * bit (< 5), element-wise, other, high bits (>= 5), kernel (0 element-wise,
+ * 1 direct single-gate sweep, 2 fused pass).  *nblocks gets the pass count;
+ * at most max_blocks rows are written. */
+int qf_plan_circuit(int n, int layout, int nops, const int* op_k, const int* op_axes, const double* op_mats,
+                    int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
 
 /* ------------------------------------------------- state preparation ------ */

@@ -64,6 +64,7 @@ SIGNATURES = {
     "qf_timing_enable": (_c_int, [_c_int]),
     "qf_set_tile_kernel": (_c_int, [_c_int]),
     "qf_set_gate_merging": (_c_int, [_c_int]),
+    "qf_plan_circuit": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_int, _vp]),
     "qf_timing_collect": (_c_int, [_dp, ctypes.POINTER(ctypes.c_int64), _c_int]),
     "qf_sample_workspace_bytes": (_sz, [_c_int]),
     "qf_fill_basis": (_c_int, [_vp, _c_int, _c_int, _c_i64, _vp]),

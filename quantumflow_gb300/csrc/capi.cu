@@ -25,6 +25,8 @@ int batch_qaoa(const qf_batch_instance* inst, int ninst, int nlarge, const uint8
 int qaoa_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
               const double* gamma, const double* node_theta, double* out, void* ws, cudaStream_t stream);
 int wave_min_qubits(int layout);
+int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks,
+               int* nblocks);
 int wave_plan(const qf_batch_instance* hinst, int ninst, int layout, void* host_plan, size_t host_bytes,
               size_t* need_host, size_t* need_device);
 int wave_prepare(const void* host_plan, const uint8_t* edges, void* ws, size_t ws_bytes, cudaStream_t stream);
@@ -193,6 +195,28 @@ int qf_run_circuit(const void* psi_in, void* psi_out, int n, int layout, int nop
     mo += size_t(2) << (2 * k);
   }
   return run_ops(psi_in, psi_out, n, layout, ops, fusion_k, as_stream(stream), passes);
+}
+
+int qf_plan_circuit(int n, int layout, int nops, const int* op_k, const int* op_axes, const double* op_mats,
+                    int fusion_k, int32_t* stats, int max_blocks, int* nblocks) {
+  if (!valid_layout(layout)) return QF_ERR_LAYOUT;
+  if (n < 1 || n > QF_MAX_QUBITS) return QF_ERR_INVALID_ARGUMENT;
+  if (nops < 0 || nblocks == nullptr || max_blocks < 0 || (max_blocks > 0 && stats == nullptr))
+    return QF_ERR_INVALID_ARGUMENT;
+  if (nops > 0 && (op_k == nullptr || op_axes == nullptr || op_mats == nullptr)) return QF_ERR_INVALID_ARGUMENT;
+  std::vector<HostOp> ops(nops);
+  size_t ax = 0, mo = 0;
+  for (int i = 0; i < nops; ++i) {
+    const int k = op_k[i];
+    int bits[QF_MAX_GATE_QUBITS];
+    int rc = axes_to_bits(n, k, op_axes + ax, bits);
+    if (rc) return rc;
+    rc = classify_op(k, bits, op_mats + mo, ops[i]);
+    if (rc) return rc;
+    ax += k;
+    mo += size_t(2) << (2 * k);
+  }
+  return plan_stats(n, layout, ops, fusion_k, stats, max_blocks, nblocks);
 }
 
 int qf_cut_values(uint16_t* cuts, int n, int nedges, const int* edges, void* stream) {

@@ -762,34 +762,58 @@ QF_D void lswap_dispatch(int l, int j, int lane, E (&a)[1 << RB]) {
 template <int RB, typename E>
 QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t xb,
                       const int64_t (&hoff)[1 << RB], E (&a)[1 << RB]) {
+  constexpr int R = 1 << RB;
+  // Sign ops (CZ-like) first, as one parity mask over the registers: the
+  // part of a mask outside the register bits is tested once per thread,
+  // only register bits per register (all ops of a segment are diagonal and
+  // commute, so the signs can be applied last).
+  const int64_t regbits = hoff[R - 1];
+  uint32_t negmask = 0;
+  bool other = false;
+  for (int o = in.a; o < in.a + in.b; ++o) {
+    const SegOp& so = P.segs[o];
+    if (so.type != OP_SIGN) {
+      other = true;
+      continue;
+    }
+    const uint64_t m = so.mask, mreg = m & (uint64_t)regbits, mout = m & ~mreg;
+    if (((uint64_t)xb & mout) != mout) continue;
+    if (mreg == 0) {
+      negmask ^= (1u << R) - 1u;
+    } else {
 #pragma unroll
-  for (int r = 0; r < (1 << RB); ++r) {
+      for (int r = 0; r < R; ++r)
+        if (((uint64_t)hoff[r] & mreg) == mreg) negmask ^= 1u << r;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
     const int64_t x = xb | hoff[r];
     E v = a[r];
-    bool neg = false;
-    for (int o = in.a; o < in.a + in.b; ++o) {
-      const SegOp& so = P.segs[o];
-      switch (so.type) {
-        case OP_SIGN:
-          neg ^= ((uint64_t)x & so.mask) == so.mask;
-          break;
-        case OP_DIAG: {
-          int idx = 0;
-          for (int i = 0; i < so.k; ++i) idx = (idx << 1) | int((x >> so.gb[i]) & 1);
-          v = cmul_v(scoef[so.coef + idx], v);
-          break;
+    if (other) {
+      for (int o = in.a; o < in.a + in.b; ++o) {
+        const SegOp& so = P.segs[o];
+        switch (so.type) {
+          case OP_DIAG: {
+            int idx = 0;
+            for (int i = 0; i < so.k; ++i) idx = (idx << 1) | int((x >> so.gb[i]) & 1);
+            v = cmul_v(scoef[so.coef + idx], v);
+            break;
+          }
+          case OP_CUT: {
+            const int c = min((int)P.cuts[x], so.ncoef - 1);
+            v = cmul_v(scoef[so.coef + c], v);
+            break;
+          }
+          case OP_PHASE:
+            v = cmul_v(scoef[so.coef], v);
+            break;
+          default:
+            break;
         }
-        case OP_CUT: {
-          const int c = min((int)P.cuts[x], so.ncoef - 1);
-          v = cmul_v(scoef[so.coef + c], v);
-          break;
-        }
-        case OP_PHASE:
-          v = cmul_v(scoef[so.coef], v);
-          break;
       }
     }
-    a[r] = neg ? cneg(v) : v;
+    a[r] = ((negmask >> r) & 1u) ? cneg(v) : v;
   }
 }
 
@@ -1817,22 +1841,21 @@ void merge_ops(std::vector<HostOp>& ops, int n) {
 int g_default_fusion[3] = {4, 2, 2};  // per layout (C64, C128, FF): warp-tile capacity
 int g_merge_gates = 1;                 // qf_set_gate_merging
 
-int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
-            cudaStream_t stream, int* passes_out) {
+struct PlanBlock {
+  std::vector<int> idx;
+  uint64_t hmask = 0;
+  int ncoef = 0;
+  bool elem_only = true;
+};
+
+// Gate merging, then greedy blocking into passes (see above); host only.
+static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int layout, int& fusion_k) {
   const int Lmin = 5;  // bits 0..4 are the lane bits of every fused kernel
   if (fusion_k <= 0) fusion_k = g_default_fusion[layout];
   if (fusion_k > 8) fusion_k = 8;
   if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
-  int passes = 0;
-  const void* src = in;
-  struct Block {
-    std::vector<int> idx;
-    uint64_t hmask = 0;
-    int ncoef = 0;
-    bool elem_only = true;
-  };
-  std::vector<Block> blocks;
-  Block cur;
+  std::vector<PlanBlock> blocks;
+  PlanBlock cur;
   for (int i = 0; i < (int)ops.size(); ++i) {
     const HostOp& op = ops[i];
     const int need = coef_count(op);
@@ -1846,7 +1869,7 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
                       cur.ncoef + need <= (cur.elem_only ? TILE_MAX_COEF / 2 : TILE_MAX_COEF);
     if (!cur.idx.empty() && !fits) {
       blocks.push_back(cur);
-      cur = Block();
+      cur = PlanBlock();
     }
     cur.idx.push_back(i);
     cur.hmask |= bits;
@@ -1854,6 +1877,45 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
     cur.elem_only = cur.elem_only && is_elementwise(op.type);
   }
   if (!cur.idx.empty()) blocks.push_back(cur);
+  return blocks;
+}
+
+// Per planned pass: ops, dense 1-qubit, dense 2-qubit (of which with a lane
+// bit), element-wise, other, high bits, kernel (0 element-wise, 1 direct
+// single-gate sweep, 2 fused pass).
+int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks,
+               int* nblocks) {
+  std::vector<PlanBlock> blocks = plan_blocks(ops, n, layout, fusion_k);
+  *nblocks = (int)blocks.size();
+  for (int b = 0; b < (int)blocks.size() && b < max_blocks; ++b) {
+    const PlanBlock& B = blocks[b];
+    int32_t* st = stats + 8 * b;
+    std::memset(st, 0, 8 * sizeof(int32_t));
+    st[0] = (int32_t)B.idx.size();
+    for (int i : B.idx) {
+      const HostOp& op = ops[i];
+      if (op.type == OP_DENSE1) st[1]++;
+      else if (op.type == OP_DENSE2) {
+        st[2]++;
+        if (op.gb[0] < 5 || op.gb[1] < 5) st[3]++;
+      } else if (is_elementwise(op.type)) st[4]++;
+      else st[5]++;
+    }
+    st[6] = __builtin_popcountll(B.hmask & ~uint64_t(31));
+    const HostOp& first = ops[B.idx[0]];
+    st[7] = B.elem_only ? 0
+            : (B.idx.size() == 1 && (first.type == OP_DENSE1 || first.type == OP_MONO || first.type == OP_DENSE2))
+                ? 1 : 2;
+  }
+  return QF_OK;
+}
+
+int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
+            cudaStream_t stream, int* passes_out) {
+  const int Lmin = 5;
+  std::vector<PlanBlock> blocks = plan_blocks(ops, n, layout, fusion_k);
+  int passes = 0;
+  const void* src = in;
   if (blocks.empty()) {
     if (in != out) {
       const size_t bytes = (size_t(1) << n) * elem_bytes(layout);
@@ -1864,7 +1926,7 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
     if (passes_out) *passes_out = passes;
     return QF_OK;
   }
-  for (const Block& b : blocks) {
+  for (const PlanBlock& b : blocks) {
     int rc;
     const HostOp& first = ops[b.idx[0]];
     if (b.elem_only) {
