@@ -139,3 +139,40 @@ def test_graph6_reads_reference_datasets():
         assert len(ours) == len(theirs) == 100
         for g, G in zip(ours, theirs):
             assert {tuple(sorted(e)) for e in g.edges()} == {tuple(sorted(e)) for e in G.edges()}
+
+
+def test_plan_circuit_host_only():
+    """The pass planner runs on the host: gate merging turns U.CZ.U of two
+    random layers into one dense 2-qubit block per matched pair, and every
+    high bit of a pass fits the warp tile."""
+    import ctypes
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(1)
+    N = 12
+    circ = qf.Circuit()
+    for layer in range(4):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
+
+    def plan(merge):
+        nat.lib.qf_set_gate_merging(merge)
+        stats = np.zeros(8 * 512, np.int32)
+        nb = ctypes.c_int()
+        rc = nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                     op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb))
+        assert rc == 0
+        return stats[:8 * nb.value].reshape(-1, 8)
+
+    try:
+        merged, plain = plan(1), plan(0)
+    finally:
+        nat.lib.qf_set_gate_merging(1)
+    assert plain[:, 0].sum() == nops                 # every gate planned once
+    assert merged[:, 0].sum() < nops                 # merging removed gates
+    assert merged[:, 2].sum() >= N // 2                # dense 4x4 blocks from U.CZ.U
+    assert len(merged) < len(plain)
+    assert (merged[:, 6] <= 2).all() and set(merged[:, 7]) <= {0, 1, 2}
