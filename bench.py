@@ -296,7 +296,8 @@ def main():
     ap.add_argument("--fusion", type=int, default=0, help="0 = library default per element type")
     ap.add_argument("--seed", type=int, default=2018)
     ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
-    ap.add_argument("--merge", type=int, default=1, choices=[0, 1], help="qf_set_gate_merging (1 = default)")
+    ap.add_argument("--merge", type=int, default=1, choices=[0, 1, 2],
+                    help="qf_set_gate_merging: 1 merge (default), 2 merge + pass packing, 0 off")
     ap.add_argument("--no-qaoa", action="store_true", help="skip the QAOA time-to-ratio measurement")
     ap.add_argument("--qaoa-graphs", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
@@ -462,7 +463,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": f"random-layer circuit N={N}, {args.layers} layers x (Haar U(2) on "
                                    f"every qubit + CZ on a seeded perfect matching), {ngates} gates, "
-                                   f"fusion k={args.fusion}, gate merging {'on' if args.merge else 'off'}",
+                                   f"fusion k={args.fusion}, gate merging {['off', 'on', 'on, passes packed'][args.merge]}",
                        "state_bytes": S * 2 ** N, "l2": "state larger than L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},
             "gate_apps_per_s": world * ngates / (ms * 1e-3),

@@ -89,9 +89,11 @@ int qf_timing_enable(int on);
  * float-float, 3 or 4 for complex64, else their default). */
 int qf_set_tile_kernel(int mode);
 /* Gate merging before pass planning (diagnostics and tests; no reference
- * counterpart), process-wide: 1 = on (default) -- consecutive gates are
- * multiplied into blocks of at most two qubits on the host whenever
- * fusion_k > 1; 0 = every gate is applied as given. */
+ * counterpart), process-wide, whenever fusion_k > 1: 1 (default) =
+ * consecutive gates are multiplied into blocks of at most two qubits on the
+ * host; 2 = merging, then re-ordering within the gates' dependences to pack
+ * each pass with as many gates as its high-bit budget allows; 0 = every
+ * gate is applied as given. */
 int qf_set_gate_merging(int on);
 /* The pass plan qf_run_circuit would execute, without touching the GPU
  * (diagnostics; no reference counterpart).  For each planned pass, 8 ints

@@ -107,7 +107,7 @@ int qf_set_tile_kernel(int mode) {
 }
 
 int qf_set_gate_merging(int on) {
-  if (on != 0 && on != 1) return QF_ERR_INVALID_ARGUMENT;
+  if (on < 0 || on > 2) return QF_ERR_INVALID_ARGUMENT;
   g_merge_gates = on;
   return QF_OK;
 }

@@ -168,11 +168,14 @@ def test_gate_merging_equals_unmerged_and_oracle(N, dtype, fusion_k, tile_kernel
     try:
         nat.call("qf_set_gate_merging", 1)
         merged = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k).asarray().reshape(-1)
+        nat.call("qf_set_gate_merging", 2)
+        packed = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k).asarray().reshape(-1)
         nat.call("qf_set_gate_merging", 0)
         plain = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k).asarray().reshape(-1)
     finally:
         nat.call("qf_set_gate_merging", 1)
     assert np.max(np.abs(merged - plain)) < tol
+    assert np.max(np.abs(packed - plain)) < tol
     if N <= 12:
         ops = [(g.asoperator(), tuple(g.qubits)) for g in circ]
         ref = orc.run_ops(orc.zero_state(N), ops).reshape(-1)
