@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) k_dense1_low(const typename Types<LAY>::E
 template <int LAY>
 __global__ void __launch_bounds__(256) k_dense2(const typename Types<LAY>::E* in,
                                                 typename Types<LAY>::E* out, int64_t nquads, int q0,
-                                                int q1, const __grid_constant__ CoefArr16 u) {
+                                                int q1, const __grid_constant__ CoefArr16 u, int dense) {
   using E = typename Types<LAY>::E;
   const int lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0;
   const int64_t b0 = int64_t(1) << q0, b1 = int64_t(1) << q1;
@@ -149,6 +149,13 @@ __global__ void __launch_bounds__(256) k_dense2(const typename Types<LAY>::E* in
     E a[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) a[r] = in[idx[r]];
+    if constexpr (LAY == FF) {
+      if (dense) {  // every coefficient part nonzero (merged Haar blocks): tree sums
+#pragma unroll
+        for (int r = 0; r < 4; ++r) out[idx[r]] = ff_cdot4_dense(&u.c[4 * r], a);
+        continue;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) out[idx[r]] = cdot<4>(&u.c[4 * r], a);
   }
@@ -1168,7 +1175,9 @@ static int launch_single_t(const void* in, void* out, int n, const HostOp& op, c
       CoefArr16 u;
       for (int i = 0; i < 16; ++i) u.c[i] = make_coef(op.m[i], LAY);
       const int64_t nq = int64_t(1) << (n - 2);
-      k_dense2<LAY><<<grid_for(nq), 256, 0, stream>>>(src, dst, nq, op.gb[0], op.gb[1], u);
+      int dense = 1;
+      for (int i = 0; i < 16; ++i) dense &= (op.m[i].real() != 0.0 && op.m[i].imag() != 0.0) ? 1 : 0;
+      k_dense2<LAY><<<grid_for(nq), 256, 0, stream>>>(src, dst, nq, op.gb[0], op.gb[1], u, dense);
       return check_cuda(cudaGetLastError());
     }
     case OP_MONO: {

@@ -158,6 +158,42 @@ QF_D void ff_dot2(float ah, float al, float xh, float xl, float bh, float bl, fl
   fast_two_sum(s, __fadd_rn(__fadd_rn(c0, c1), t), rh, rl);
 }
 
+// Float-float sum of eight product terms: a TwoSum tree (depth 3) on the
+// rounded products, all rounding errors and cross terms gathered in the low
+// word, one renormalisation.
+QF_D void ff_sum8(const float (&p)[8], const float (&c)[8], float& hi, float& lo) {
+  float s[4], t[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) two_sum(p[2 * i], p[2 * i + 1], s[i], t[i]);
+  float s01, t01, s23, t23, ss, tt;
+  two_sum(s[0], s[1], s01, t01);
+  two_sum(s[2], s[3], s23, t23);
+  two_sum(s01, s23, ss, tt);
+  float e = __fadd_rn(__fadd_rn(__fadd_rn(c[0], c[1]), __fadd_rn(c[2], c[3])),
+                      __fadd_rn(__fadd_rn(c[4], c[5]), __fadd_rn(c[6], c[7])));
+  e = __fadd_rn(e, __fadd_rn(__fadd_rn(__fadd_rn(t[0], t[1]), __fadd_rn(t[2], t[3])),
+                             __fadd_rn(__fadd_rn(t01, t23), tt)));
+  fast_two_sum(ss, e, hi, lo);
+}
+// sum_j u[j] a[j] over four terms with every coefficient part nonzero
+QF_D float4 ff_cdot4_dense(const Coef* u, const float4* a) {
+  float p[8], c[8];
+  float4 r;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    ff_term(u[j].f[0], u[j].f[1], a[j].x, a[j].y, p[2 * j], c[2 * j]);
+    ff_term(-u[j].f[2], -u[j].f[3], a[j].z, a[j].w, p[2 * j + 1], c[2 * j + 1]);
+  }
+  ff_sum8(p, c, r.x, r.y);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    ff_term(u[j].f[0], u[j].f[1], a[j].z, a[j].w, p[2 * j], c[2 * j]);
+    ff_term(u[j].f[2], u[j].f[3], a[j].x, a[j].y, p[2 * j + 1], c[2 * j + 1]);
+  }
+  ff_sum8(p, c, r.z, r.w);
+  return r;
+}
+
 template <int J>
 QF_D float4 cdot(const Coef* u, const float4* a) {
   if constexpr (J == 2) {
