@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 namespace qf {
 
@@ -452,7 +453,7 @@ QF_D void g1_reg_dispatch(int j, const Coef* cf, E (&a)[1 << RB]) {
 }
 
 template <int RB, int J0, int J1, typename E>
-QF_D void g2_reg(const Coef* cf, E (&a)[1 << RB]) {
+QF_D void g2_reg(const Coef* cf, E (&a)[1 << RB], bool dense = false) {
   constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
 #pragma unroll
   for (int i = 0; i < (1 << (RB - 2)); ++i) {
@@ -460,6 +461,13 @@ QF_D void g2_reg(const Coef* cf, E (&a)[1 << RB]) {
     b = ((b >> HI) << (HI + 1)) | (b & ((1 << HI) - 1));
     const int idx[4] = {b, b | (1 << J1), b | (1 << J0), b | (1 << J0) | (1 << J1)};
     E p[4] = {a[idx[0]], a[idx[1]], a[idx[2]], a[idx[3]]};
+    if constexpr (sizeof(E) == sizeof(float4) && std::is_same<E, float4>::value) {
+      if (dense) {  // every coefficient part nonzero: float-float TwoSum trees
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[idx[r]] = ff_cdot4_dense(cf + 4 * r, p);
+        continue;
+      }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) a[idx[r]] = cdot<4>(cf + 4 * r, p);
   }
@@ -917,7 +925,7 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
           break;
         case I_G2R:
           if constexpr (SWAP) {
-            if constexpr (RB >= 2) g2_reg<RB, RB - 1, RB - 2>(&P.coef[in.coef], a);
+            if constexpr (RB >= 2) g2_reg<RB, RB - 1, RB - 2>(&P.coef[in.coef], a, in.c != 0);
           } else {
             g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
           }
@@ -1635,8 +1643,10 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
         rswap(reg_pos(g0), RB - 1);
         rswap(reg_pos(g1), RB - 2);
       }
-      emit(TInstr{I_G2R, (uint8_t)(SWAP ? 0 : reg_pos(g0)), (uint8_t)(SWAP ? 0 : reg_pos(g1)), 0,
-                  (uint16_t)coef_at[i], 0});
+      bool dense = true;
+      for (int e = 0; e < 16; ++e) dense = dense && op.m[e].real() != 0.0 && op.m[e].imag() != 0.0;
+      emit(TInstr{I_G2R, (uint8_t)(SWAP ? 0 : reg_pos(g0)), (uint8_t)(SWAP ? 0 : reg_pos(g1)),
+                  (uint8_t)(dense ? 1 : 0), (uint16_t)coef_at[i], 0});
     }
   }
   // restore the lanes in order; a lane fixed here stays fixed (the bit
