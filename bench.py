@@ -66,7 +66,7 @@ def build_circuit(ops):
 # workload at N=24 complex128 (profiles/); the write shortfall is dirty L2
 # lines still resident when the kernel ends.  Scaled by the state size.
 KERNEL_TRAFFIC_N24 = {
-    "dense2": (268.476160e6, 206.269696e6),
+    "dense2": (268.485120e6, 206.819072e6),
     "warp_tile": (269.407744e6, 209.610240e6),
 }
 
