@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) k_adj(const __grid_constant__ AdjParams P
 // layer's last pass).  Each sub-tile is prefetched two sub-tiles ahead into
 // a per-warp shared-memory ring with per-thread async copies.
 constexpr int ADJW_MAX_COEF = 1100;
-constexpr int ADJW_STAGES = 3;  // per-warp prefetch ring depth (sub-tiles)
+constexpr int ADJW_STAGES = 2;  // per-warp prefetch ring depth (sub-tiles)
 
 struct AdjWParams {
   void* psi;

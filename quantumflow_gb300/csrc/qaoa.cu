@@ -56,7 +56,7 @@ void qaoa_layer_ops(int n, const uint16_t* cuts, int nedges, double beta, double
 // group order reversed on alternate layers a layer boundary costs no extra
 // pass: p layers over m groups take 1 + p (m - 1) passes.
 constexpr int QW_MAX_COEF = 1100;
-constexpr int QW_STAGES = 3;
+constexpr int QW_STAGES = 2;
 
 struct QaoaWParams {
   void* psi;
