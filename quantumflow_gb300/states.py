@@ -23,7 +23,8 @@ from . import config
 from .qubits import Qubits, qubits_count_tuple
 
 __all__ = ["State", "zero_state", "w_state", "ghz_state", "random_state", "join_states",
-           "print_state", "print_probabilities", "basis_state", "uniform_state"]
+           "print_state", "print_probabilities", "basis_state", "uniform_state",
+           "upload_state", "HostCopy"]
 
 _DTYPES = {"complex128": torch.complex128, "complex64": torch.complex64}
 
@@ -108,6 +109,43 @@ class Buffer:
         return self._complex
 
 
+_IO_STREAMS = {}
+
+
+def _io_streams(device):
+    """(upload, download) copy streams of one device, made on first use."""
+    index = torch.device(device).index
+    if index is None:
+        index = torch.cuda.current_device()
+    if index not in _IO_STREAMS:
+        with torch.cuda.device(index):
+            _IO_STREAMS[index] = (torch.cuda.Stream(), torch.cuda.Stream())
+    return _IO_STREAMS[index]
+
+
+class HostCopy:
+    """A device-to-host copy in flight (from :meth:`State.to_host`)."""
+
+    __slots__ = ("tensor", "event", "shape")
+
+    def __init__(self, tensor: torch.Tensor, event, shape):
+        self.tensor = tensor
+        self.event = event
+        self.shape = shape
+
+    def done(self) -> bool:
+        return self.event.query()
+
+    def wait(self, stream=None) -> None:
+        """Order ``stream`` (default: the current stream) after the copy."""
+        (stream or torch.cuda.current_stream()).wait_event(self.event)
+
+    def result(self) -> torch.Tensor:
+        """Block until the copy has landed; the host amplitudes as [2]*N."""
+        self.event.synchronize()
+        return self.tensor.reshape(self.shape)
+
+
 def _as_complex_tensor(tensor, dtype=None) -> torch.Tensor:
     device = _device()
     if isinstance(tensor, torch.Tensor):
@@ -177,6 +215,29 @@ class State:
 
     def asarray(self) -> np.ndarray:
         return self.tensor.detach().cpu().numpy()
+
+    def to_host(self, out: torch.Tensor = None) -> "HostCopy":
+        """Copy the amplitudes into host memory on the device's download
+        stream, after the work queued so far on the current stream, and
+        return at once: the copy overlaps whatever is launched next.  ``out``
+        (pinned, same element count and complex dtype as ``tensor``)
+        receives them; a pinned buffer is allocated when it is None.  Read
+        the result through :meth:`HostCopy.result`."""
+        t = self._buf.complex().reshape(-1)
+        if out is None:
+            out = torch.empty(t.numel(), dtype=t.dtype, pin_memory=True)
+        if (out.device.type != "cpu" or out.numel() != t.numel() or out.dtype != t.dtype
+                or not out.is_contiguous()):
+            raise ValueError("to_host wants a contiguous host tensor with the state's element count and dtype")
+        cur = torch.cuda.current_stream(t.device)
+        _, down = _io_streams(t.device)
+        down.wait_stream(cur)
+        with torch.cuda.stream(down):
+            out.reshape(-1).copy_(t, non_blocking=True)
+            event = torch.cuda.Event()
+            event.record(down)
+        t.record_stream(down)
+        return HostCopy(out, event, [2] * self._buf.n)
 
     def asdensity(self):
         """|psi><psi| as a Density (quantumflow/states.py:162-165)."""
@@ -309,6 +370,28 @@ def inner(a: State, b: State) -> complex:
 
 
 # ----------------------------------------------------------- constructors --
+def upload_state(host: torch.Tensor, qubits: Qubits = None, memory: Dict = None, *,
+                 dtype: str = None) -> State:
+    """A State from host amplitudes, copied on the device's upload stream.
+
+    The copy does not wait for work already queued on the current stream,
+    so with a pinned ``host`` it overlaps a circuit still running on the
+    device; the current stream waits for it before the returned state's
+    first use.  ``host`` must stay unchanged until that copy has run."""
+    if not isinstance(host, torch.Tensor):
+        host = torch.from_numpy(np.ascontiguousarray(np.asarray(host)))
+    if host.device.type != "cpu":
+        raise ValueError("upload_state takes host amplitudes")
+    device = _device()
+    up, _ = _io_streams(device)
+    cur = torch.cuda.current_stream(device)
+    with torch.cuda.stream(up):
+        dev = host.reshape(-1).to(device, non_blocking=True)
+    cur.wait_stream(up)
+    dev.record_stream(cur)
+    return State(dev, qubits, memory, dtype=dtype)
+
+
 def basis_state(qubits: Union[int, Qubits], index: int = 0, dtype: str = "complex128") -> State:
     N, qubits = qubits_count_tuple(qubits)
     if N == 0:  # the empty register: one amplitude, 1 (kept on the host side of the ABI)
