@@ -296,6 +296,7 @@ def main():
     ap.add_argument("--fusion", type=int, default=0, help="0 = library default per element type")
     ap.add_argument("--seed", type=int, default=2018)
     ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
+    ap.add_argument("--shape-bits", type=int, default=None, help="qf_set_shape_bits (default: library)")
     ap.add_argument("--merge", type=int, default=1, choices=[0, 1, 2],
                     help="qf_set_gate_merging: 1 merge (default), 2 merge + pass packing, 0 off")
     ap.add_argument("--no-qaoa", action="store_true", help="skip the QAOA time-to-ratio measurement")
@@ -330,6 +331,8 @@ def main():
     if args.arith:
         qf.config.C128_ARITHMETIC = args.arith
     nat.call("qf_set_tile_kernel", args.tile_mode)
+    if args.shape_bits is not None:
+        nat.call("qf_set_shape_bits", args.shape_bits)
     nat.call("qf_set_gate_merging", args.merge)
 
     N, S = args.n, (16 if args.dtype == "complex128" else 8)

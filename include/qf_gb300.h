@@ -78,16 +78,25 @@ size_t qf_reduce_workspace_bytes(int n);
 #define QF_KERNEL_PERMUTATION 3
 #define QF_KERNEL_ELEMENTWISE 4
 #define QF_KERNEL_WARP_TILE 5
-#define QF_KERNEL_CLASSES 6
+#define QF_KERNEL_GROUP 6
+#define QF_KERNEL_SHAPE 7
+#define QF_KERNEL_CLASSES 8
 int qf_timing_enable(int on);
 /* Fused-pass kernel selection (diagnostics and tests; no reference
- * counterpart), process-wide: 0 = default (warp tiles, then shared-memory
- * register programs, then the shared-memory kernel, whichever first fits
- * the block); 1 = shared-memory kernels only (gate passes and the QAOA
- * adjoint); 2, 3, 4 = default order with warp tiles of 2^mode registers per
- * thread (the adjoint's warp tiles take 2 or 3 for complex128 and
- * float-float, 3 or 4 for complex64, else their default). */
+ * counterpart), process-wide: 0 = default (float-float group passes --
+ * every thread holding the amplitudes of a pass's <= 4 gate bits -- then
+ * warp tiles, then shared-memory register programs, then the shared-memory
+ * kernel, whichever first fits the block); 1 = shared-memory kernels only
+ * (gate passes and the QAOA adjoint); 2, 3, 4 = no group passes, warp tiles
+ * of 2^mode registers per thread (the adjoint's warp tiles take 2 or 3 for
+ * complex128 and float-float, 3 or 4 for complex64, else their default);
+ * 5 = default order without group passes. */
 int qf_set_tile_kernel(int mode);
+/* Widest float-float shape pass, in gate bits (0..4; 0 = no shape passes),
+ * process-wide (tuning; no reference counterpart).  A fused pass of dense
+ * gates and CZ-like signs is cut into straight-line shape kernels of at
+ * most this many gate bits each. */
+int qf_set_shape_bits(int bits);
 /* Gate merging before pass planning (diagnostics and tests; no reference
  * counterpart), process-wide, whenever fusion_k > 1: 1 (default) =
  * consecutive gates are multiplied into blocks of at most two qubits on the

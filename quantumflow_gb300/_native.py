@@ -63,6 +63,7 @@ SIGNATURES = {
     "qf_reduce_workspace_bytes": (_sz, [_c_int]),
     "qf_timing_enable": (_c_int, [_c_int]),
     "qf_set_tile_kernel": (_c_int, [_c_int]),
+    "qf_set_shape_bits": (_c_int, [_c_int]),
     "qf_set_gate_merging": (_c_int, [_c_int]),
     "qf_plan_circuit": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_int, _vp]),
     "qf_timing_collect": (_c_int, [_dp, ctypes.POINTER(ctypes.c_int64), _c_int]),
@@ -155,7 +156,7 @@ def device_error(stream=None):
     return flags.value
 
 
-KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile")
+KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile", "group", "shape")
 
 
 def timing_enable(on=True):

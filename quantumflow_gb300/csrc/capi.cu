@@ -14,6 +14,8 @@ extern int g_force_smem_tile;
 extern int g_adjoint_smem_only;
 extern int g_warp_rb_override;
 extern int g_merge_gates;
+extern int g_group_kernel;
+extern int g_shape_max_bits;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
                const double* gamma, const double* node_theta, int fusion_k, cudaStream_t stream);
@@ -98,11 +100,18 @@ int qf_get_device_error(int* flags, void* stream) {
   return read_clear_device_error(flags, as_stream(stream));
 }
 
+int qf_set_shape_bits(int bits) {
+  if (bits < 0 || bits > 4) return QF_ERR_INVALID_ARGUMENT;
+  g_shape_max_bits = bits;
+  return QF_OK;
+}
+
 int qf_set_tile_kernel(int mode) {
-  if (mode < 0 || mode > 4) return QF_ERR_INVALID_ARGUMENT;
+  if (mode < 0 || mode > 5) return QF_ERR_INVALID_ARGUMENT;
   g_force_smem_tile = mode == 1;
   g_adjoint_smem_only = mode == 1;
-  g_warp_rb_override = mode >= 2 ? mode : 0;
+  g_warp_rb_override = mode >= 2 && mode <= 4 ? mode : 0;
+  g_group_kernel = mode == 5 ? 0 : 1;
   return QF_OK;
 }
 

@@ -7,6 +7,7 @@
 // quantumflow/circuits.py:87-99 Circuit.run does.  Nothing here is a
 // translation of that einsum: the state is swept once per fused block.
 #include "engine.cuh"
+#include "regops.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -429,65 +430,6 @@ QF_D void regs_store(E* s, const TMap& m, const E (&a)[1 << RB], int lane, int w
   const int base = lane | warp_local(m, warp);
 #pragma unroll
   for (int r = 0; r < (1 << RB); ++r) s[base | reg_local<RB>(m, r)] = a[r];
-}
-
-template <int RB, int J, typename E>
-QF_D void g1_reg(const Coef* cf, E (&a)[1 << RB]) {
-#pragma unroll
-  for (int i = 0; i < (1 << (RB - 1)); ++i) {
-    const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
-    const int i1 = i0 | (1 << J);
-    E p[2] = {a[i0], a[i1]};
-    a[i0] = cdot<2>(cf, p);
-    a[i1] = cdot<2>(cf + 2, p);
-  }
-}
-template <int RB, typename E>
-QF_D void g1_reg_dispatch(int j, const Coef* cf, E (&a)[1 << RB]) {
-  switch (j) {
-    case 0: g1_reg<RB, 0>(cf, a); break;
-    case 1: if constexpr (RB > 1) g1_reg<RB, 1>(cf, a); break;
-    case 2: if constexpr (RB > 2) g1_reg<RB, 2>(cf, a); break;
-    case 3: if constexpr (RB > 3) g1_reg<RB, 3>(cf, a); break;
-  }
-}
-
-template <int RB, int J0, int J1, typename E>
-QF_D void g2_reg(const Coef* cf, E (&a)[1 << RB], bool dense = false) {
-  constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
-#pragma unroll
-  for (int i = 0; i < (1 << (RB - 2)); ++i) {
-    int b = ((i >> LO) << (LO + 1)) | (i & ((1 << LO) - 1));
-    b = ((b >> HI) << (HI + 1)) | (b & ((1 << HI) - 1));
-    const int idx[4] = {b, b | (1 << J1), b | (1 << J0), b | (1 << J0) | (1 << J1)};
-    E p[4] = {a[idx[0]], a[idx[1]], a[idx[2]], a[idx[3]]};
-    if constexpr (sizeof(E) == sizeof(float4) && std::is_same<E, float4>::value) {
-      if (dense) {  // every coefficient part nonzero: float-float TwoSum trees
-#pragma unroll
-        for (int r = 0; r < 4; ++r) a[idx[r]] = ff_cdot4_dense(cf + 4 * r, p);
-        continue;
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) a[idx[r]] = cdot<4>(cf + 4 * r, p);
-  }
-}
-template <int RB, typename E>
-QF_D void g2_reg_dispatch(int j0, int j1, const Coef* cf, E (&a)[1 << RB]) {
-  switch (j0 * 4 + j1) {
-    case 1: g2_reg<RB, 0, 1>(cf, a); break;
-    case 4: g2_reg<RB, 1, 0>(cf, a); break;
-    case 2: if constexpr (RB > 2) g2_reg<RB, 0, 2>(cf, a); break;
-    case 8: if constexpr (RB > 2) g2_reg<RB, 2, 0>(cf, a); break;
-    case 6: if constexpr (RB > 2) g2_reg<RB, 1, 2>(cf, a); break;
-    case 9: if constexpr (RB > 2) g2_reg<RB, 2, 1>(cf, a); break;
-    case 3: if constexpr (RB > 3) g2_reg<RB, 0, 3>(cf, a); break;
-    case 12: if constexpr (RB > 3) g2_reg<RB, 3, 0>(cf, a); break;
-    case 7: if constexpr (RB > 3) g2_reg<RB, 1, 3>(cf, a); break;
-    case 13: if constexpr (RB > 3) g2_reg<RB, 3, 1>(cf, a); break;
-    case 11: if constexpr (RB > 3) g2_reg<RB, 2, 3>(cf, a); break;
-    case 14: if constexpr (RB > 3) g2_reg<RB, 3, 2>(cf, a); break;
-  }
 }
 
 template <int RB, typename E>
@@ -1858,6 +1800,14 @@ void merge_ops(std::vector<HostOp>& ops, int n) {
 // block unconditionally (they need no tile bits), every other op joins while
 // the union of high bits (>= Lmin) stays within fusion_k.
 int g_default_fusion[3] = {4, 2, 2};  // per layout (C64, C128, FF): warp-tile capacity
+int g_group_kernel = 1;               // qf_set_tile_kernel(5) turns the group kernel off
+
+// Group passes are the default fused kernel for the passes they fit; the
+// diagnostic kernel selections (forced shared-memory tiles, warp register
+// widths) and tile mode 5 leave them out.
+static bool group_pass_enabled() {
+  return g_group_kernel && !g_force_smem_tile && g_warp_rb_override == 0;
+}
 int g_merge_gates = 1;                 // qf_set_gate_merging: 0 off, 1 merge, 2 merge + pack passes
 
 // Pass packing (optional, qf_set_gate_merging(2)): after merging, the gates
@@ -1938,6 +1888,51 @@ struct PlanBlock {
   bool elem_only = true;
 };
 
+// Float-float fused passes of dense gates and sign ops are cut where their
+// next dense gate would leave the shape table (group.cu), so that each
+// piece runs as one straight-line shape kernel: on this layout a pass is
+// bound by FP32 issue, and two such sweeps cost less than one interpreted
+// pass over both gates.  Blocks with other ops stay whole.
+static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<HostOp>& ops) {
+  std::vector<PlanBlock> out;
+  out.reserve(blocks.size());
+  for (PlanBlock& b : blocks) {
+    bool ok = !b.elem_only && b.idx.size() > 1;
+    for (int i : b.idx) {
+      const uint8_t t = ops[i].type;
+      ok = ok && (t == OP_DENSE1 || t == OP_DENSE2 || t == OP_SIGN);
+    }
+    if (!ok) {
+      out.push_back(std::move(b));
+      continue;
+    }
+    PlanBlock cur;
+    int dense[3], nd = 0;
+    auto close = [&]() {
+      if (!cur.idx.empty()) out.push_back(std::move(cur));
+      cur = PlanBlock();
+      nd = 0;
+    };
+    for (int i : b.idx) {
+      const HostOp& op = ops[i];
+      if (op.type != OP_SIGN) {
+        dense[nd] = i;
+        if (nd > 0 && (nd == 2 || shape_of(ops, dense, nd + 1) < 0)) {
+          close();
+          dense[0] = i;
+        }
+        ++nd;
+        cur.elem_only = false;
+        for (int j = 0; j < op.k; ++j) cur.hmask |= uint64_t(1) << op.gb[j];
+      }
+      cur.idx.push_back(i);
+      cur.ncoef += coef_count(op);
+    }
+    close();
+  }
+  blocks.swap(out);
+}
+
 // Gate merging, then greedy blocking into passes (see above); host only.
 static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int layout, int& fusion_k) {
   const int Lmin = 5;  // bits 0..4 are the lane bits of every fused kernel
@@ -1968,12 +1963,14 @@ static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int l
     cur.elem_only = cur.elem_only && is_elementwise(op.type);
   }
   if (!cur.idx.empty()) blocks.push_back(cur);
+  if (layout == FF && group_pass_enabled()) split_for_shapes(blocks, ops);
   return blocks;
 }
 
 // Per planned pass: ops, dense 1-qubit, dense 2-qubit (of which with a lane
 // bit), element-wise, other, high bits, kernel (0 element-wise, 1 direct
-// single-gate sweep, 2 fused pass).
+// single-gate sweep, 2 fused warp-tile or shared-memory pass, 3 group pass,
+// 4 shape pass).
 int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks,
                int* nblocks) {
   std::vector<PlanBlock> blocks = plan_blocks(ops, n, layout, fusion_k);
@@ -1997,6 +1994,13 @@ int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_
     st[7] = B.elem_only ? 0
             : (B.idx.size() == 1 && (first.type == OP_DENSE1 || first.type == OP_MONO || first.type == OP_DENSE2))
                 ? 1 : 2;
+    static thread_local GroupParams gp;
+    static thread_local ShapeParams sp;
+    int G = 0;
+    if (st[7] == 2 && group_pass_enabled()) {
+      if (shape_prepare(n, layout, ops, B.idx, sp) == QF_OK) st[7] = 4;
+      else if (group_prepare(n, layout, ops, B.idx, gp, G) == QF_OK) st[7] = 3;
+    }
   }
   return QF_OK;
 }
@@ -2033,7 +2037,20 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
       int hb = __builtin_popcountll(b.hmask & ~((uint64_t(1) << Lmin) - 1));
       int rb = g_warp_rb_override > 0 ? g_warp_rb_override : warp_rb(layout);
       rc = QF_ERR_NOT_SUPPORTED;
-      if (!g_force_smem_tile && hb <= rb) {
+      static thread_local GroupParams gp;  // ~11 KiB: kept off the stack
+      static thread_local ShapeParams sp;
+      int G = 0;
+      if (group_pass_enabled() && shape_prepare(n, layout, ops, b.idx, sp) == QF_OK) {
+        sp.in = src;
+        sp.out = out;
+        LaunchTimer timer(QF_KERNEL_SHAPE, stream);
+        rc = shape_launch(sp, stream);
+      } else if (group_pass_enabled() && group_prepare(n, layout, ops, b.idx, gp, G) == QF_OK) {
+        gp.in = src;
+        gp.out = out;
+        LaunchTimer timer(QF_KERNEL_GROUP, stream);
+        rc = group_launch(gp, G, stream);
+      } else if (!g_force_smem_tile && hb <= rb) {
         LaunchTimer timer(QF_KERNEL_WARP_TILE, stream);
         rc = launch_warp_block(src, out, n, layout, ops, b.idx, rb, stream);
       }

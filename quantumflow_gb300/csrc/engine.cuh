@@ -166,6 +166,73 @@ int launch_tile_block(const void* in, void* out, int n, int layout, const std::v
                       const std::vector<int>& idx, uint64_t hmask, cudaStream_t stream);
 int launch_single(const void* in, void* out, int n, int layout, const HostOp& op, cudaStream_t stream);
 
+// Group passes (k_group, float-float layout): a fused pass whose dense
+// gates touch at most four bits.  Every thread holds the 2^G amplitudes
+// that differ only in those G bits (register-index bit j = global bit
+// rbits[j]), applies the pass's ops to them in order and writes them back;
+// sign ops (CZ-like) become one per-thread register mask, applied before
+// the next dense gate.
+constexpr int GROUP_MAX_OPS = 96;
+constexpr int GROUP_MAX_COEF = 512;
+struct GroupOp {
+  uint8_t type;    // OP_DENSE1 / OP_DENSE2 / OP_SIGN / OP_DIAG / OP_PHASE
+  uint8_t a, b;    // dense: register-index bits (DENSE2: a = matrix MSB, a > b)
+  uint8_t flag;    // DENSE2: every coefficient part nonzero; DIAG: k
+  uint8_t flush;   // dense: apply the pending sign mask first
+  uint8_t gb[3];   // DIAG: global bits, matrix MSB first
+  uint16_t coef;   // first coefficient
+  uint16_t rmask;  // SIGN: registers whose group bits of the op are all set
+  uint32_t pad;
+  uint64_t mout;   // SIGN: the op's global bits outside the group
+};
+struct GroupParams {
+  const void* in;
+  void* out;
+  int32_t n, nops;
+  int32_t final_flush, pad;
+  uint8_t rbits[4];  // global bit of register-index bit j
+  uint8_t sbits[4];  // the same bits, ascending
+  int64_t off[16];   // global offset of register index r
+  GroupOp ops[GROUP_MAX_OPS];
+  Coef coef[GROUP_MAX_COEF];
+};
+// Fill P for the pass ops[idx] and return QF_OK with its group size G, or
+// QF_ERR_NOT_SUPPORTED when the pass does not fit a group kernel.
+int group_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::vector<int>& idx,
+                  GroupParams& P, int& G);
+int group_launch(const GroupParams& P, int G, cudaStream_t stream);
+
+// Shape passes (k_shape, float-float layout): the straight-line form of a
+// group pass for the common programs -- one or two dense gates (slots) on
+// fixed register bits, with sign ops (CZ-like) between and around them as
+// per-thread register masks.  The host renames the pass's gate bits to
+// register bits in order of first use (top first), which maps every
+// program of the table in group.cu to one compiled kernel.
+constexpr int SHAPE_MAX_SIGNS = 64;
+struct ShapeParams {
+  const void* in;
+  void* out;
+  int32_t n, shape;
+  int32_t sign_end[3];  // signs [sign_end[b-1], sign_end[b]) act before slot b (b = 2: after the last)
+  int32_t pad;
+  uint8_t sbits[4];     // the group bits, ascending
+  uint8_t dense[2];     // slot s: every coefficient part nonzero
+  uint8_t pad2[2];
+  int64_t off[16];      // global offset of register index r
+  uint16_t rmask[SHAPE_MAX_SIGNS];
+  uint64_t mout[SHAPE_MAX_SIGNS];
+  Coef coef[32];        // slot s at coef[16 s]
+};
+// Which table shape the dense ops ops[dense[0..nd)] form (-1: none); the
+// planner splits fused float-float passes at the points where the next
+// dense gate would leave the table.
+int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd);
+// Fill P for the pass ops[idx] (dense gates and sign ops only) and launch
+// it; QF_ERR_NOT_SUPPORTED when it is not a table shape.
+int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::vector<int>& idx,
+                  ShapeParams& P);
+int shape_launch(const ShapeParams& P, cudaStream_t stream);
+
 int device_sm_count();
 int timing_enable(int on);
 int timing_collect(double* ms, int64_t* counts, int nkinds);

@@ -205,3 +205,58 @@ def test_gate_merging_random_layers_n20():
         finally:
             nat.call("qf_set_gate_merging", 1)
         assert np.max(np.abs(merged - plain)) < tol
+
+
+@pytest.mark.parametrize("merge", [0, 1])
+def test_shape_passes_random_programs(merge):
+    """Float-float fused passes split into straight-line shape kernels (one
+    or two dense gates with CZ signs around them): random programs of Haar
+    1- and 2-qubit gates and CZs, mostly on the low (lane) bits where the
+    fused passes form, against the oracle, with shapes of up to three
+    (default) and four gate bits, and against the same programs without
+    group/shape passes (tile mode 5)."""
+    import ctypes
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    N = 12
+    rng = np.random.default_rng(77 + merge)
+    low = list(range(N - 5, N))  # axes of bits 0..4
+    nat.call("qf_set_gate_merging", merge)
+    seen_shapes = 0
+    try:
+        for trial in range(24):
+            circ = qf.Circuit()
+            for _ in range(int(rng.integers(6, 30))):
+                pick = rng.random()
+                qs = [int(q) for q in rng.choice(low if rng.random() < 0.8 else range(N), 2, replace=False)]
+                if pick < 0.35:
+                    circ += qf.random_gate([qs[0]], random_state=rng)
+                elif pick < 0.65:
+                    circ += qf.random_gate(qs, random_state=rng)
+                else:
+                    circ += qf.CZ(*qs)
+            op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
+            stats = np.zeros(8 * 256, np.int32)
+            nb = ctypes.c_int()
+            assert nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                           op_mats.ctypes.data, 0, stats.ctypes.data, 256, ctypes.byref(nb)) == 0
+            seen_shapes += int((stats[:8 * nb.value].reshape(-1, 8)[:, 7] == 4).sum())
+            got = circ.run(qf.zero_state(N)).asarray().reshape(-1)
+            ops = [(g.asoperator(), tuple(g.qubits)) for g in circ]
+            ref = orc.run_ops(orc.zero_state(N), ops).reshape(-1)
+            assert np.max(np.abs(got - ref)) < 1e-12, trial
+            nat.call("qf_set_shape_bits", 4)  # the four-bit shape as well
+            try:
+                wide = circ.run(qf.zero_state(N)).asarray().reshape(-1)
+            finally:
+                nat.call("qf_set_shape_bits", 3)
+            assert np.max(np.abs(wide - ref)) < 1e-12, trial
+            nat.call("qf_set_tile_kernel", 5)
+            try:
+                old = circ.run(qf.zero_state(N)).asarray().reshape(-1)
+            finally:
+                nat.call("qf_set_tile_kernel", 0)
+            assert np.max(np.abs(got - old)) < 1e-12, trial
+    finally:
+        nat.call("qf_set_gate_merging", 1)
+    assert seen_shapes >= 10

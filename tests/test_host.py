@@ -175,4 +175,16 @@ def test_plan_circuit_host_only():
     assert merged[:, 0].sum() < nops                 # merging removed gates
     assert merged[:, 2].sum() >= N // 2                # dense 4x4 blocks from U.CZ.U
     assert len(merged) < len(plain)
-    assert (merged[:, 6] <= 2).all() and set(merged[:, 7]) <= {0, 1, 2}
+    assert (merged[:, 6] <= 2).all() and set(merged[:, 7]) <= {0, 1, 2, 3, 4}
+    # float-float fused passes of dense gates and CZ signs become shape passes
+    # (kernel 4): one or two dense gates each, no other ops
+    shape = merged[merged[:, 7] == 4]
+    assert len(shape) > 0
+    assert ((shape[:, 1] + shape[:, 2]) >= 1).all() and ((shape[:, 1] + shape[:, 2]) <= 2).all()
+    assert (shape[:, 5] == 0).all()
+    nat.lib.qf_set_tile_kernel(5)  # default order without group or shape passes
+    try:
+        assert not {3, 4} & set(plan(1)[:, 7])
+    finally:
+        nat.lib.qf_set_tile_kernel(0)
+        nat.lib.qf_set_gate_merging(1)
