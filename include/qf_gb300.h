@@ -92,10 +92,11 @@ int qf_timing_enable(int on);
  * complex128 and float-float, 3 or 4 for complex64, else their default);
  * 5 = default order without group passes. */
 int qf_set_tile_kernel(int mode);
-/* Widest float-float shape pass, in gate bits (0..4; 0 = no shape passes),
+/* Widest float-float shape pass, in gate bits (0..4, default 3),
  * process-wide (tuning; no reference counterpart).  A fused pass of dense
  * gates and CZ-like signs is cut into straight-line shape kernels of at
- * most this many gate bits each. */
+ * most this many gate bits each; 0 = no shape passes (fused passes stay
+ * whole and run the interpreted group or warp-tile kernels). */
 int qf_set_shape_bits(int bits);
 /* Gate merging before pass planning (diagnostics and tests; no reference
  * counterpart), process-wide, whenever fusion_k > 1: 1 (default) =

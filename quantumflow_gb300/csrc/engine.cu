@@ -1808,6 +1808,17 @@ int g_group_kernel = 1;               // qf_set_tile_kernel(5) turns the group k
 static bool group_pass_enabled() {
   return g_group_kernel && !g_force_smem_tile && g_warp_rb_override == 0;
 }
+// The interpreted group kernel takes passes of dense gates and signs only
+// (measured 21% faster than warp tiles on unmerged layers of 2x2 gates and
+// CZs at N=26); passes with diagonal phases (QFT's CPHASE) stay on warp
+// tiles, which were 2.7% faster there.
+static bool group_pass_fits(const std::vector<HostOp>& ops, const std::vector<int>& idx) {
+  for (int i : idx) {
+    const uint8_t t = ops[i].type;
+    if (t != OP_DENSE1 && t != OP_DENSE2 && t != OP_SIGN) return false;
+  }
+  return true;
+}
 int g_merge_gates = 1;                 // qf_set_gate_merging: 0 off, 1 merge, 2 merge + pack passes
 
 // Pass packing (optional, qf_set_gate_merging(2)): after merging, the gates
@@ -1890,18 +1901,25 @@ struct PlanBlock {
 
 // Float-float fused passes of dense gates and sign ops are cut where their
 // next dense gate would leave the shape table (group.cu), so that each
-// piece runs as one straight-line shape kernel: on this layout a pass is
-// bound by FP32 issue, and two such sweeps cost less than one interpreted
-// pass over both gates.  Blocks with other ops stay whole.
+// piece runs as one straight-line shape kernel: on this layout a pass with
+// a 4x4 gate is bound by FP32 issue, and two such sweeps cost less than one
+// interpreted pass over both gates.  Blocks with other ops, and blocks of
+// more than two 2x2 gates without a 4x4, stay whole.
 static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<HostOp>& ops) {
   std::vector<PlanBlock> out;
   out.reserve(blocks.size());
   for (PlanBlock& b : blocks) {
     bool ok = !b.elem_only && b.idx.size() > 1;
+    int nd1 = 0, nd2 = 0;
     for (int i : b.idx) {
       const uint8_t t = ops[i].type;
       ok = ok && (t == OP_DENSE1 || t == OP_DENSE2 || t == OP_SIGN);
+      nd1 += t == OP_DENSE1;
+      nd2 += t == OP_DENSE2;
     }
+    // a pass of 2x2 gates alone is cheap per gate: splitting more than two
+    // of them would add sweeps that are bound by HBM, not by arithmetic
+    if (nd2 == 0 && nd1 > 2) ok = false;
     if (!ok) {
       out.push_back(std::move(b));
       continue;
@@ -1963,7 +1981,7 @@ static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int l
     cur.elem_only = cur.elem_only && is_elementwise(op.type);
   }
   if (!cur.idx.empty()) blocks.push_back(cur);
-  if (layout == FF && group_pass_enabled()) split_for_shapes(blocks, ops);
+  if (layout == FF && group_pass_enabled() && g_shape_max_bits > 0) split_for_shapes(blocks, ops);
   return blocks;
 }
 
@@ -1999,7 +2017,7 @@ int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_
     int G = 0;
     if (st[7] == 2 && group_pass_enabled()) {
       if (shape_prepare(n, layout, ops, B.idx, sp) == QF_OK) st[7] = 4;
-      else if (group_prepare(n, layout, ops, B.idx, gp, G) == QF_OK) st[7] = 3;
+      else if (group_pass_fits(ops, B.idx) && group_prepare(n, layout, ops, B.idx, gp, G) == QF_OK) st[7] = 3;
     }
   }
   return QF_OK;
@@ -2045,7 +2063,8 @@ int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& o
         sp.out = out;
         LaunchTimer timer(QF_KERNEL_SHAPE, stream);
         rc = shape_launch(sp, stream);
-      } else if (group_pass_enabled() && group_prepare(n, layout, ops, b.idx, gp, G) == QF_OK) {
+      } else if (group_pass_enabled() && group_pass_fits(ops, b.idx) &&
+                 group_prepare(n, layout, ops, b.idx, gp, G) == QF_OK) {
         gp.in = src;
         gp.out = out;
         LaunchTimer timer(QF_KERNEL_GROUP, stream);

@@ -232,6 +232,7 @@ int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd);
 int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::vector<int>& idx,
                   ShapeParams& P);
 int shape_launch(const ShapeParams& P, cudaStream_t stream);
+extern int g_shape_max_bits;  // qf_set_shape_bits (0: no shape passes, blocks stay whole)
 
 int device_sm_count();
 int timing_enable(int on);
