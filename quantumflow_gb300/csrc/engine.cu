@@ -1809,9 +1809,9 @@ static bool group_pass_enabled() {
   return g_group_kernel && !g_force_smem_tile && g_warp_rb_override == 0;
 }
 // The interpreted group kernel takes passes of dense gates and signs only
-// (measured 21% faster than warp tiles on unmerged layers of 2x2 gates and
-// CZs at N=26); passes with diagonal phases (QFT's CPHASE) stay on warp
-// tiles, which were 2.7% faster there.
+// (those the shape split leaves whole, or all of them when shape passes are
+// off); passes with diagonal phases (QFT's CPHASE) stay on warp tiles, which
+// ran QFT at N=26 in 87.7 ms against 90.1 ms on the group kernel.
 static bool group_pass_fits(const std::vector<HostOp>& ops, const std::vector<int>& idx) {
   for (int i : idx) {
     const uint8_t t = ops[i].type;
@@ -1901,25 +1901,21 @@ struct PlanBlock {
 
 // Float-float fused passes of dense gates and sign ops are cut where their
 // next dense gate would leave the shape table (group.cu), so that each
-// piece runs as one straight-line shape kernel: on this layout a pass with
-// a 4x4 gate is bound by FP32 issue, and two such sweeps cost less than one
-// interpreted pass over both gates.  Blocks with other ops, and blocks of
-// more than two 2x2 gates without a 4x4, stay whole.
+// piece runs as one straight-line shape kernel: on this layout a pass is
+// bound by FP32 issue, and two such sweeps cost less than one interpreted
+// pass over both gates (also for passes of 2x2 gates alone: unmerged layers
+// of 2x2 gates and CZs at N=26 ran 23.7 ms split against 29.9 ms on warp
+// tiles and 119.3 against 114.6 ms per 10 merged random layers at N=28 when
+// such passes stayed whole).  Blocks with other ops stay whole.
 static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<HostOp>& ops) {
   std::vector<PlanBlock> out;
   out.reserve(blocks.size());
   for (PlanBlock& b : blocks) {
     bool ok = !b.elem_only && b.idx.size() > 1;
-    int nd1 = 0, nd2 = 0;
     for (int i : b.idx) {
       const uint8_t t = ops[i].type;
       ok = ok && (t == OP_DENSE1 || t == OP_DENSE2 || t == OP_SIGN);
-      nd1 += t == OP_DENSE1;
-      nd2 += t == OP_DENSE2;
     }
-    // a pass of 2x2 gates alone is cheap per gate: splitting more than two
-    // of them would add sweeps that are bound by HBM, not by arithmetic
-    if (nd2 == 0 && nd1 > 2) ok = false;
     if (!ok) {
       out.push_back(std::move(b));
       continue;
