@@ -136,18 +136,19 @@ __global__ void __launch_bounds__(256) k_dense1_low(const typename Types<LAY>::E
   }
 }
 
-// 2-qubit dense gate on bits q0 (matrix MSB) and q1.
-template <int LAY>
+// 2-qubit dense gate on bits q0 (matrix MSB) and q1.  IT: the index type
+// (uint32_t for states of at most 2^31 amplitudes, int64_t above).
+template <int LAY, typename IT>
 __global__ void __launch_bounds__(256) k_dense2(const typename Types<LAY>::E* in,
-                                                typename Types<LAY>::E* out, int64_t nquads, int q0,
+                                                typename Types<LAY>::E* out, IT nquads, int q0,
                                                 int q1, const __grid_constant__ CoefArr16 u, int dense) {
   using E = typename Types<LAY>::E;
   const int lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0;
-  const int64_t b0 = int64_t(1) << q0, b1 = int64_t(1) << q1;
-  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nquads; t += nthr) {
-    const int64_t base = insert0(insert0(t, lo), hi);
-    const int64_t idx[4] = {base, base | b1, base | b0, base | b0 | b1};
+  const IT b0 = IT(1) << q0, b1 = IT(1) << q1;
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < nquads; t += nthr) {
+    const IT base = insert0(insert0(t, lo), hi);
+    const IT idx[4] = {base, base | b1, base | b0, base | b0 | b1};
     E a[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) a[r] = in[idx[r]];
@@ -1127,7 +1128,11 @@ static int launch_single_t(const void* in, void* out, int n, const HostOp& op, c
       const int64_t nq = int64_t(1) << (n - 2);
       int dense = 1;
       for (int i = 0; i < 16; ++i) dense &= (op.m[i].real() != 0.0 && op.m[i].imag() != 0.0) ? 1 : 0;
-      k_dense2<LAY><<<grid_for(nq), 256, 0, stream>>>(src, dst, nq, op.gb[0], op.gb[1], u, dense);
+      if (n <= 31)
+        k_dense2<LAY, uint32_t><<<grid_for(nq), 256, 0, stream>>>(src, dst, (uint32_t)nq, op.gb[0], op.gb[1], u,
+                                                                  dense);
+      else
+        k_dense2<LAY, int64_t><<<grid_for(nq), 256, 0, stream>>>(src, dst, nq, op.gb[0], op.gb[1], u, dense);
       return check_cuda(cudaGetLastError());
     }
     case OP_MONO: {

@@ -261,24 +261,25 @@ QF_D void slot_apply(const Coef* cf, float4 (&v)[1 << G], bool dense) {
   }
 }
 
-template <int G, int S0, int S1>
+// IT: index type (uint32_t for states of at most 2^31 amplitudes)
+template <int G, int S0, int S1, typename IT>
 __global__ void __launch_bounds__(256) k_shape(const __grid_constant__ ShapeParams P) {
   constexpr int R = 1 << G;
   const float4* gin = reinterpret_cast<const float4*>(P.in);
   float4* gout = reinterpret_cast<float4*>(P.out);
-  const int64_t ngroups = int64_t(1) << (P.n - G);
-  const int64_t nthr = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
-    int64_t xb = t;
+  const IT ngroups = IT(1) << (P.n - G);
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
+    IT xb = t;
 #pragma unroll
     for (int j = 0; j < G; ++j) xb = insert0(xb, P.sbits[j]);
     float4 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = gin[xb | P.off[r]];
+    for (int r = 0; r < R; ++r) v[r] = gin[xb | (IT)P.off[r]];
     auto signs = [&](int s0, int s1) {
       uint32_t m = 0;
       for (int s = s0; s < s1; ++s)
-        if ((xb & (int64_t)P.mout[s]) == (int64_t)P.mout[s]) m ^= P.rmask[s];
+        if ((xb & (IT)P.mout[s]) == (IT)P.mout[s]) m ^= P.rmask[s];
       apply_negmask<R>(m, v);
     };
     if (P.sign_end[0] > 0) signs(0, P.sign_end[0]);
@@ -289,17 +290,21 @@ __global__ void __launch_bounds__(256) k_shape(const __grid_constant__ ShapePara
     }
     if (P.sign_end[2] > P.sign_end[1]) signs(P.sign_end[1], P.sign_end[2]);
 #pragma unroll
-    for (int r = 0; r < R; ++r) gout[xb | P.off[r]] = v[r];
+    for (int r = 0; r < R; ++r) gout[xb | (IT)P.off[r]] = v[r];
   }
 }
 
 using ShapeKernel = void (*)(ShapeParams);
-static const ShapeKernel kShapeKernels[kNumShapes] = {
-    k_shape<1, 10, 0>,   k_shape<2, 110, 0>,   k_shape<1, 10, 10>,   k_shape<2, 11, 10>,
-    k_shape<2, 11, 110>, k_shape<3, 12, 110>,  k_shape<2, 110, 11>,  k_shape<2, 110, 10>,
-    k_shape<3, 121, 10>, k_shape<2, 110, 110>, k_shape<3, 121, 120>, k_shape<3, 121, 110>,
-    k_shape<4, 132, 110>,
-};
+#define QF_SHAPES(IT)                                                                                 \
+  {                                                                                                  \
+    k_shape<1, 10, 0, IT>, k_shape<2, 110, 0, IT>, k_shape<1, 10, 10, IT>, k_shape<2, 11, 10, IT>,       \
+        k_shape<2, 11, 110, IT>, k_shape<3, 12, 110, IT>, k_shape<2, 110, 11, IT>,                     \
+        k_shape<2, 110, 10, IT>, k_shape<3, 121, 10, IT>, k_shape<2, 110, 110, IT>,                    \
+        k_shape<3, 121, 120, IT>, k_shape<3, 121, 110, IT>, k_shape<4, 132, 110, IT>,                  \
+  }
+static const ShapeKernel kShapeKernels32[kNumShapes] = QF_SHAPES(uint32_t);
+static const ShapeKernel kShapeKernels64[kNumShapes] = QF_SHAPES(int64_t);
+#undef QF_SHAPES
 
 // Register naming of a dense-op program: bits in order of first use get
 // register bits G-1, G-2, ...; codes[] the slot codes; swap[s] when a 4x4
@@ -438,7 +443,7 @@ int shape_launch(const ShapeParams& P, cudaStream_t stream) {
   const int64_t cap = (int64_t)device_sm_count() * 8;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  kShapeKernels[P.shape]<<<(int)grid, 256, 0, stream>>>(P);
+  (P.n <= 31 ? kShapeKernels32 : kShapeKernels64)[P.shape]<<<(int)grid, 256, 0, stream>>>(P);
   return check_cuda(cudaGetLastError());
 }
 

@@ -296,6 +296,11 @@ QF_HD int64_t insert0(int64_t v, int b) {
   const int64_t lo = v & ((int64_t(1) << b) - 1);
   return ((v >> b) << (b + 1)) | lo;
 }
+// 32-bit form for states of at most 2^31 amplitudes (b <= 30)
+QF_HD uint32_t insert0(uint32_t v, int b) {
+  const uint32_t lo = v & ((1u << b) - 1u);
+  return ((v >> b) << (b + 1)) | lo;
+}
 
 
 // ------------------------------------ per-amplitude helpers (all layouts) --

@@ -260,3 +260,46 @@ def test_shape_passes_random_programs(merge):
     finally:
         nat.call("qf_set_gate_merging", 1)
     assert seen_shapes >= 10
+
+
+def test_index_paths_above_2_31_amplitudes():
+    """States of more than 2^31 amplitudes take the 64-bit-index forms of the
+    4x4 sweep and the shape kernels: N=32 float-float (64 GB per state,
+    128 GB at the peak), two merged random layers and their inverse must
+    return |0...0> -- norm and single-qubit marginals by device reductions,
+    no host copy of the state."""
+    import ctypes
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    from quantumflow_gb300.states import _reduce
+    N = 32
+    free, _ = torch.cuda.mem_get_info()
+    if free < 150 * 2 ** 30:
+        pytest.skip("needs 150 GB of free device memory")
+    rng = np.random.default_rng(32)
+    circ = qf.Circuit()
+    for layer in range(2):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    for q in range(N):
+        circ += qf.random_gate([q], random_state=rng)
+    op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
+    stats = np.zeros(8 * 512, np.int32)
+    nb = ctypes.c_int()
+    assert nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                   op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
+    kinds = set(stats[:8 * nb.value].reshape(-1, 8)[:, 7])
+    assert {1, 4} <= kinds  # lone sweeps and shape passes both run
+    ket = circ.run(qf.zero_state(N))
+    assert abs(ket.norm() - 1) < 1e-11
+    back = circ.H.run(ket)
+    del ket
+    assert abs(back.norm() - 1) < 1e-11
+    for axis in (0, 7, 26, 31):
+        p0, p1 = _reduce("qf_qubit_probabilities", back.buffer, nout=2, extra=(axis,))
+        assert abs(p0 - 1) < 1e-11 and abs(p1) < 1e-11
+    del back
+    torch.cuda.empty_cache()
