@@ -188,3 +188,40 @@ def test_plan_circuit_host_only():
     finally:
         nat.lib.qf_set_tile_kernel(0)
         nat.lib.qf_set_gate_merging(1)
+
+
+def test_shape_width_splits_passes():
+    """The shape-width setting (qf_set_shape_bits) decides where a fused
+    float-float pass is cut: two 4x4 gates on four distinct lane bits are one
+    four-bit shape pass at width 4, two single-gate passes at the default
+    width 3, and one interpreted pass with shapes off (width 0)."""
+    import ctypes
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    N = 12
+    rng = np.random.default_rng(3)
+    # axes N-1..N-4 are bits 0..3 (lane bits); CZs keep the gates unmerged
+    circ = qf.Circuit([qf.random_gate([N - 1, N - 2], random_state=rng), qf.CZ(N - 1, 0),
+                       qf.random_gate([N - 3, N - 4], random_state=rng)])
+    op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
+
+    def plan():
+        stats = np.zeros(8 * 64, np.int32)
+        nb = ctypes.c_int()
+        assert nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                       op_mats.ctypes.data, 0, stats.ctypes.data, 64, ctypes.byref(nb)) == 0
+        return stats[:8 * nb.value].reshape(-1, 8)
+
+    try:
+        assert nat.lib.qf_set_shape_bits(4) == 0
+        wide = plan()
+        assert len(wide) == 1 and wide[0, 7] == 4 and wide[0, 2] == 2
+        assert nat.lib.qf_set_shape_bits(3) == 0
+        default = plan()
+        assert len(default) == 2 and set(default[:, 7]) <= {1, 4} and default[:, 2].sum() == 2
+        assert nat.lib.qf_set_shape_bits(0) == 0
+        off = plan()
+        assert len(off) == 1 and off[0, 7] == 3  # the interpreted group kernel
+        assert nat.lib.qf_set_shape_bits(5) != 0  # out of range
+    finally:
+        nat.lib.qf_set_shape_bits(3)
