@@ -303,3 +303,18 @@ def test_index_paths_above_2_31_amplitudes():
         assert abs(p0 - 1) < 1e-11 and abs(p1) < 1e-11
     del back
     torch.cuda.empty_cache()
+
+
+def test_gops_benchmark_tool():
+    """The GOPS benchmark (tools/benchmark.py): gate by gate and fused give
+    the same state; the oracle agrees at N=10; GOPS is positive."""
+    from quantumflow_gb300 import benchmark as bm
+    N, gates = 10, 100
+    a = bm.benchmark(N, gates, fused=False, seed=5).cpu().numpy().reshape(-1)
+    b = bm.benchmark(N, gates, fused=True, seed=5).cpu().numpy().reshape(-1)
+    assert np.max(np.abs(a - b)) < 1e-12
+    circ = bm.benchmark_circuit(N, gates, seed=5)
+    assert len(list(circ)) == N + 3 * ((gates - N) // 3)
+    ref = orc.run_ops(orc.zero_state(N), [(g.asoperator(), tuple(g.qubits)) for g in circ]).reshape(-1)
+    assert np.max(np.abs(a - ref)) < 1e-12
+    assert bm.benchmark_gops(N, gates, 1) > 0 and bm.benchmark_gops(N, gates, 1, fused=True) > 0

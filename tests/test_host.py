@@ -225,3 +225,16 @@ def test_shape_width_splits_passes():
         assert nat.lib.qf_set_shape_bits(5) != 0  # out of range
     finally:
         nat.lib.qf_set_shape_bits(3)
+
+
+def test_gops_benchmark_circuit():
+    """tools/benchmark.py's circuit: H on every qubit, then X, T, CNOT
+    triples on random distinct qubit pairs (host only)."""
+    from quantumflow_gb300 import benchmark as bm
+    circ = list(bm.benchmark_circuit(16, 100, seed=1))
+    assert len(circ) == 16 + 3 * 28
+    assert [type(g).__name__ for g in circ[:16]] == ["H"] * 16
+    for i in range(16, len(circ), 3):
+        x, t, cnot = circ[i:i + 3]
+        assert (type(x).__name__, type(t).__name__, type(cnot).__name__) == ("X", "T", "CNOT")
+        assert cnot.qubits == (x.qubits[0], t.qubits[0]) and x.qubits != t.qubits
