@@ -238,3 +238,44 @@ def test_gops_benchmark_circuit():
         x, t, cnot = circ[i:i + 3]
         assert (type(x).__name__, type(t).__name__, type(cnot).__name__) == ("X", "T", "CNOT")
         assert cnot.qubits == (x.qubits[0], t.qubits[0]) and x.qubits != t.qubits
+
+
+def test_shape_split_keeps_every_op():
+    """Cutting fused passes into shapes only re-partitions the op list: over
+    random programs, every shape width (0, 2, 3, 4) plans the same merged ops
+    (same totals per op class), and no shape pass holds more than two dense
+    gates."""
+    import ctypes
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    N = 13
+    rng = np.random.default_rng(11)
+    try:
+        for trial in range(12):
+            circ = qf.Circuit()
+            for _ in range(int(rng.integers(10, 60))):
+                qs = [int(q) for q in rng.choice(N, 2, replace=False)]
+                pick = rng.random()
+                if pick < 0.35:
+                    circ += qf.random_gate([qs[0]], random_state=rng)
+                elif pick < 0.6:
+                    circ += qf.random_gate(qs, random_state=rng)
+                elif pick < 0.9:
+                    circ += qf.CZ(*qs)
+                else:
+                    circ += qf.RZ(float(rng.uniform(0, 3)), qs[0])
+            op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
+            totals = []
+            for bits in (0, 2, 3, 4):
+                assert nat.lib.qf_set_shape_bits(bits) == 0
+                stats = np.zeros(8 * 512, np.int32)
+                nb = ctypes.c_int()
+                assert nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                               op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
+                s = stats[:8 * nb.value].reshape(-1, 8)
+                totals.append(tuple(s[:, :6].sum(0)))
+                shape = s[s[:, 7] == 4]
+                assert ((shape[:, 1] + shape[:, 2]) <= 2).all()
+            assert len(set(totals)) == 1, totals
+    finally:
+        nat.lib.qf_set_shape_bits(3)
