@@ -113,7 +113,7 @@ class AngleGNN:
         nat.call("qf_adam_update", nat.ptr(self.params), nat.ptr(grad), nat.ptr(self.m), nat.ptr(self.v),
                  self.nparams, lr, betas[0], betas[1], eps, self.step, nat.stream_handle(self.device))
 
-    # ------------------------------------------------------------ driver ---
+    # ------------------------------------------------------------- use ---
     def predict(self, graphs) -> np.ndarray:
         """Angles (len(graphs), 2p): beta_0..beta_{p-1}, gamma_0..gamma_{p-1}."""
         batch = graphs if isinstance(graphs, GraphBatch) else GraphBatch(graphs, self.device)

@@ -283,14 +283,14 @@ def qaoa_fixtures(qf, rng):
     from quantumflow.qaoa import qubo_circuit, graph_cuts
     out = {}
     cases = []
-    # C1: G(6, 0.5) from a seed, p=5, angles U[0, pi)
-    cases.append(("c1", nx.gnp_random_graph(6, 0.5, seed=7), 5, True))
-    # 3-regular graphs (C3 shape at oracle-friendly n) and ER graphs
+    # the MAXCUT example size: G(6, 0.5) from a seed, p=5, angles U[0, pi)
+    cases.append(("er6p5", nx.gnp_random_graph(6, 0.5, seed=7), 5, True))
+    # 3-regular graphs (the gradient workload's family at oracle-friendly n) and ER graphs
     cases.append(("reg8", nx.random_regular_graph(3, 8, seed=11), 3, True))
     cases.append(("reg10", nx.random_regular_graph(3, 10, seed=12), 8, True))
     cases.append(("er9", nx.gnp_random_graph(9, 0.5, seed=13), 2, True))
     cases.append(("reg12", nx.random_regular_graph(3, 12, seed=14), 2, False))
-    # config 3 at oracle-friendly size: 3-regular n=16, p=8 (state not stored)
+    # the n=24, p=8 gradient workload at oracle-friendly size: 3-regular n=16, p=8 (state not stored)
     cases.append(("reg16p8", nx.random_regular_graph(3, 16, seed=16), 8, True))
     # weighted edges + node weights (RZ quirk, qaoa.py:55-58)
     g = nx.gnp_random_graph(7, 0.6, seed=21)
@@ -342,11 +342,11 @@ def qaoa_fixtures(qf, rng):
         names.append(name)
     out["qaoa_cases"] = np.array(names)
 
-    # C1 driver semantics: 5 gradient-ascent steps on <C>, lr=0.1, FD grads
+    # the example training loop (examples/qaoa_maxcut.py): 5 gradient-ascent steps on <C>, lr=0.1, FD grads
     graph = cases[0][1]
     p = 5
-    beta = out["c1_beta"].copy()
-    gamma = out["c1_gamma"].copy()
+    beta = out["er6p5_beta"].copy()
+    gamma = out["er6p5_gamma"].copy()
     cuts = graph_cuts(graph)
     traj = []
     for step in range(5):
@@ -364,10 +364,10 @@ def qaoa_fixtures(qf, rng):
         gamma = gamma + 0.1 * gg
         beta = beta + 0.1 * gb
         traj.append(_expect(qf, graph, p, beta, gamma, cuts))
-    out["c1_gd_expectations"] = np.array(traj)
-    out["c1_gd_beta"] = beta
-    out["c1_gd_gamma"] = gamma
-    out["c1_maxcut"] = np.array(float(np.max(cuts)))
+    out["er6p5_gd_expectations"] = np.array(traj)
+    out["er6p5_gd_beta"] = beta
+    out["er6p5_gd_gamma"] = gamma
+    out["er6p5_maxcut"] = np.array(float(np.max(cuts)))
     return out
 
 

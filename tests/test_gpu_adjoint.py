@@ -1,6 +1,6 @@
 """Adjoint gradient of QAOA MAXCUT against central finite differences of the
 reference (tests/golden, computed by the reference's numpy backend) and of
-the CPU oracle, plus torch.autograd and the gradient-ascent driver."""
+the CPU oracle, plus torch.autograd and the gradient-ascent loop (maxcut_qaoa)."""
 import numpy as np
 import pytest
 import torch
@@ -22,7 +22,7 @@ def _graph(q, name):
 def test_adjoint_vs_reference_fd(golden, dtype, tol):
     import quantumflow_gb300 as qf
     q = golden["qaoa"]
-    for name in ("c1", "reg8", "reg10", "er9", "reg16p8"):
+    for name in ("er6p5", "reg8", "reg10", "er9", "reg16p8"):
         g = _graph(q, name)
         p = int(q[f"{name}_p"])
         prob = qf.QAOAMaxCut(g, p, dtype=dtype)
@@ -90,19 +90,19 @@ def test_autograd_function():
     np.testing.assert_allclose(-gamma.grad.numpy(), gg, atol=1e-12)
 
 
-def test_c1_gradient_ascent_matches_reference(golden):
+def test_er6p5_gradient_ascent_matches_reference(golden):
     """Config 1: 5 gradient-ascent steps at lr 0.1 from the golden angles."""
     import quantumflow_gb300 as qf
     q = golden["qaoa"]
-    g = _graph(q, "c1")
-    prob = qf.QAOAMaxCut(g, int(q["c1_p"]))
-    beta, gamma = q["c1_beta"].copy(), q["c1_gamma"].copy()
+    g = _graph(q, "er6p5")
+    prob = qf.QAOAMaxCut(g, int(q["er6p5_p"]))
+    beta, gamma = q["er6p5_beta"].copy(), q["er6p5_gamma"].copy()
     traj = []
     for _ in range(5):
         e, gb, gg = prob.expectation_and_grad(beta, gamma)
         beta, gamma = beta + 0.1 * gb, gamma + 0.1 * gg
         traj.append(prob.expectation(beta, gamma))
-    np.testing.assert_allclose(traj, q["c1_gd_expectations"], atol=1e-7)
+    np.testing.assert_allclose(traj, q["er6p5_gd_expectations"], atol=1e-7)
 
 
 def test_maxcut_qaoa_star_graph():

@@ -119,7 +119,7 @@ def test_batch_wave_graph_replay():
 def test_batch_reference_fixtures(golden):
     import quantumflow_gb300 as qf
     q = golden["qaoa"]
-    names = ["c1", "reg8", "reg10", "er9", "reg16p8"]
+    names = ["er6p5", "reg8", "reg10", "er9", "reg16p8"]
     graphs = []
     for name in names:
         g = qf.Graph(nodes=range(int(q[f"{name}_n"])))

@@ -11,7 +11,7 @@ from oracle import qf_oracle as orc
 pytestmark = pytest.mark.gpu
 
 # tolerances: complex128 (FP64 and float-float arithmetic) 1e-12 max amplitude
-# error, complex64 1e-5 (spec parity bar)
+# error, complex64 1e-5 (the parity bar of this backend)
 TOL = {0: 1e-5, 1: 1e-12, 2: 1e-12}
 LAYOUTS = [0, 1, 2]
 

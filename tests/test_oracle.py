@@ -71,18 +71,18 @@ def test_random_layer_circuits(golden):
         np.testing.assert_allclose(st, c[f"rc{N}_state"], atol=1e-12)
 
 
-def test_c1_gradient_ascent(golden):
+def test_er6p5_gradient_ascent(golden):
     # examples/qaoa_maxcut.py:37-87 semantics with FD gradients, lr 0.1, 5 steps
     q = golden["qaoa"]
-    n, p = int(q["c1_n"]), int(q["c1_p"])
-    edges = [tuple(e) for e in q["c1_edges"]]
-    beta, gamma = q["c1_beta"].copy(), q["c1_gamma"].copy()
+    n, p = int(q["er6p5_n"]), int(q["er6p5_p"])
+    edges = [tuple(e) for e in q["er6p5_edges"]]
+    beta, gamma = q["er6p5_beta"].copy(), q["er6p5_gamma"].copy()
     traj = []
     for _ in range(5):
         gg, gb = orc.qaoa_fd_gradient(n, edges, p, beta, gamma)
         gamma, beta = gamma + 0.1 * gg, beta + 0.1 * gb
         traj.append(orc.qaoa_expectation(n, edges, p, beta, gamma))
-    np.testing.assert_allclose(traj, q["c1_gd_expectations"], atol=1e-8)
+    np.testing.assert_allclose(traj, q["er6p5_gd_expectations"], atol=1e-8)
 
 
 def test_oracle_matches_reference_programs(golden):
