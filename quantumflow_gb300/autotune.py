@@ -5,7 +5,8 @@ the fastest is stored under a key of (GPU name, workload signature) in
 ``~/.cache/quantumflow_gb300/autotune.json`` (override the path with
 ``QUANTUMFLOW_GB300_AUTOTUNE_CACHE``).  Lookups never tune implicitly:
 ``batch_config`` / ``fusion_config`` return cached values or ``{}`` (library
-defaults); ``tune_batch`` / ``tune_fusion`` measure and store.
+defaults); ``tune_batch`` / ``tune_fusion`` measure and store;
+``use_fusion_config`` applies a fusion result.
 """
 import hashlib
 import json
@@ -106,21 +107,48 @@ def fusion_config(dtype, n):
     return _load().get(_fusion_key(dtype, n), {})
 
 
-def tune_fusion(circuit, n, dtype="complex128", candidates=(1, 2, 3, 4, 5, 6), modes=(0, 1), reps=2):
-    """Time Circuit.run over fusion widths and fused-kernel modes
-    (qf_set_tile_kernel) on ``circuit``; stores and returns the fastest."""
+DEFAULT_SHAPE_BITS = 3  # the library's qf_set_shape_bits default
+
+
+def tune_fusion(circuit, n, dtype="complex128", candidates=(1, 2, 3, 4, 5, 6), modes=(0, 1), reps=2,
+                shape_bits=None):
+    """Time Circuit.run over fusion widths, fused-kernel modes
+    (qf_set_tile_kernel) and, for float-float complex128 states, shape
+    widths (qf_set_shape_bits; default candidates 2, 3, 4) on ``circuit``;
+    stores and returns the fastest {"fusion_k", "mode", "shape_bits", "ms",
+    "trials"}.  The process-wide settings are restored afterwards; apply a
+    result with ``use_fusion_config``."""
     from . import _native as nat
+    from . import config
     from .states import zero_state
+    ff = dtype == "complex128" and config.C128_ARITHMETIC == "ff"
+    if shape_bits is None:
+        shape_bits = (2, 3, 4) if ff else (DEFAULT_SHAPE_BITS,)
     trials = []
     best = None
-    for mode in modes:
-        nat.call("qf_set_tile_kernel", mode)
-        for k in candidates:
-            ms = _time(lambda: circuit.run(zero_state(n, dtype=dtype), fusion_k=k), reps)
-            trials.append({"fusion_k": k, "mode": mode, "ms": ms})
-            if best is None or ms < best["ms"]:
-                best = dict(trials[-1])
-    nat.call("qf_set_tile_kernel", 0)
+    try:
+        for mode in modes:
+            nat.call("qf_set_tile_kernel", mode)
+            for bits in shape_bits:
+                nat.call("qf_set_shape_bits", bits)
+                for k in candidates:
+                    ms = _time(lambda: circuit.run(zero_state(n, dtype=dtype), fusion_k=k), reps)
+                    trials.append({"fusion_k": k, "mode": mode, "shape_bits": bits, "ms": ms})
+                    if best is None or ms < best["ms"]:
+                        best = dict(trials[-1])
+    finally:
+        nat.call("qf_set_tile_kernel", 0)
+        nat.call("qf_set_shape_bits", DEFAULT_SHAPE_BITS)
     best["trials"] = trials
     _store(_fusion_key(dtype, n), best)
     return best
+
+
+def use_fusion_config(cfg):
+    """Apply a ``tune_fusion`` / ``fusion_config`` result process-wide (tile
+    mode and shape width) and return its fusion width for Circuit.run
+    (None, the library default, for an empty config)."""
+    from . import _native as nat
+    nat.call("qf_set_tile_kernel", int(cfg.get("mode", 0)))
+    nat.call("qf_set_shape_bits", int(cfg.get("shape_bits", DEFAULT_SHAPE_BITS)))
+    return cfg.get("fusion_k")

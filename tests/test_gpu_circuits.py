@@ -318,3 +318,34 @@ def test_gops_benchmark_tool():
     ref = orc.run_ops(orc.zero_state(N), [(g.asoperator(), tuple(g.qubits)) for g in circ]).reshape(-1)
     assert np.max(np.abs(a - ref)) < 1e-12
     assert bm.benchmark_gops(N, gates, 1) > 0 and bm.benchmark_gops(N, gates, 1, fused=True) > 0
+
+
+def test_autotune_fusion_and_shape_width(tmp_path, monkeypatch):
+    """tune_fusion searches fusion width, kernel mode and (float-float)
+    shape width on the caller's circuit, caches the winner, restores the
+    process-wide settings, and use_fusion_config applies it; the result of
+    the tuned configuration equals the default's."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import autotune
+    monkeypatch.setenv("QUANTUMFLOW_GB300_AUTOTUNE_CACHE", str(tmp_path / "at.json"))
+    N = 13
+    rng = np.random.default_rng(4)
+    circ = qf.Circuit()
+    for layer in range(3):
+        for q in range(N):
+            circ += qf.random_gate([q], random_state=rng)
+        perm = rng.permutation(N)
+        for a in range(0, N - 1, 2):
+            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    best = autotune.tune_fusion(circ, N, candidates=(0, 2), modes=(0,), reps=1)
+    assert {t["shape_bits"] for t in best["trials"]} == {2, 3, 4}
+    cached = autotune.fusion_config("complex128", N)
+    assert (cached["fusion_k"], cached["mode"], cached["shape_bits"]) == \
+        (best["fusion_k"], best["mode"], best["shape_bits"])
+    ref = circ.run(qf.zero_state(N)).asarray()
+    try:
+        k = autotune.use_fusion_config(best)
+        got = circ.run(qf.zero_state(N), fusion_k=k).asarray()
+    finally:
+        autotune.use_fusion_config({})
+    assert np.max(np.abs(got - ref)) < 1e-12
