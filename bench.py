@@ -10,11 +10,16 @@ Reported (one JSON line on rank 0):
   value      effective gate GB/s = gates x (2 * 16 * 2^N bytes) / step time,
              i.e. the HBM bandwidth an unfused simulator would need to match
              this speed (fusion can lift it above the HBM peak);
-  roofline   the dominant kernel (fused tile pass): bytes actually moved per
-             launch (2 * 16 * 2^N) / its mean CUDA-event duration, against the
-             measured HBM copy bandwidth;
+  roofline   the kernel class with the most time (on this workload the
+             merged dense 4x4 sweep): bytes moved per launch (2 * 16 * 2^N)
+             / its mean CUDA-event duration, against the measured HBM copy
+             bandwidth;
   e2e        the same metric through the public API with the initial state
-             copied from pinned host memory and the final state read back;
+             uploaded from pinned host memory and the final state read back
+             every step, on the library's copy streams;
+  qaoa       QAOA MAXCUT time to ratio 0.90 (learned start + batched adjoint
+             against plain start + per-graph adjoint), the batched evaluation
+             times and the single-instance adjoint gradient rate;
   cpu_baseline  the CPU oracle (numpy einsum, the reference numpy backend's
              algorithm) on a bounded sample of the same circuit family.
 
