@@ -25,3 +25,7 @@ from .programs import *  # noqa: F401,F403
 from .qaoa import qubo_circuit, graph_cuts, QAOAMaxCut, QAOAExpectation, Graph, maxcut_qaoa  # noqa: F401
 from . import qaoa  # noqa: F401
 from . import batched, autotune, gnn, adjoint, datasets  # noqa: F401
+# ``qf.backend`` is the reference's backend-module interface
+# (quantumflow/backend/__init__.py:25-35: tensormul, inner, astensor, ...),
+# here over the kernels
+from . import refbackend as backend  # noqa: F401

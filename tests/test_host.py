@@ -279,3 +279,17 @@ def test_shape_split_keeps_every_op():
             assert len(set(totals)) == 1, totals
     finally:
         nat.lib.qf_set_shape_bits(3)
+
+
+def test_backend_module_interface():
+    """``qf.backend`` exposes the reference backend-module names
+    (quantumflow/backend/__init__.py:25-35) as the reference package does."""
+    import quantumflow_gb300 as qf
+    required = ["tensormul", "inner", "outer", "astensor", "astensorproduct", "evaluate", "rank", "size",
+                "reshape", "transpose", "conj", "absolute", "real", "imag", "sum", "matmul", "diag", "trace",
+                "productdiag", "getitem", "ccast", "fcast", "cis", "exp", "cos", "sin", "sqrt", "arccos",
+                "minimum", "einsum", "set_random_seed", "gpu_available", "TL", "CTYPE", "FTYPE", "TENSOR",
+                "DEVICE", "MAX_QUBITS", "EINSUM_SUBSCRIPTS", "BKTensor", "TensorLike", "name", "version"]
+    missing = [n for n in required if not hasattr(qf.backend, n)]
+    assert not missing, missing
+    assert qf.backend.MAX_QUBITS >= 32
