@@ -35,8 +35,11 @@ def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k, tile_kern
     for N in (4, 6, 9, 12):
         circ = _circuit_from_fixture(c, N)
         ket = circ.run(qf.zero_state(N, dtype=dtype), fusion_k=fusion_k)
-        err = np.max(np.abs(ket.asarray().reshape(-1) - c[f"rc{N}_state"]))
+        got = ket.asarray().reshape(-1)
+        err = np.max(np.abs(got - c[f"rc{N}_state"]))
         assert err < tol, (N, err)
+        # fidelity against the reference's FP64 state
+        assert 1 - orc.fidelity(got.astype(np.complex128), c[f"rc{N}_state"]) < 10 * tol, N
         back = circ.H.run(ket, fusion_k=fusion_k)
         err = np.max(np.abs(back.asarray().reshape(-1) - c[f"rc{N}_inverse"]))
         assert err < tol * 2, (N, err)
