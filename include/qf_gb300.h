@@ -109,8 +109,9 @@ int qf_set_gate_merging(int on);
  * (diagnostics; no reference counterpart).  For each planned pass, 8 ints
  * in stats[8*b ..]: ops, dense 1-qubit, dense 2-qubit, of those with a lane
  * bit (< 5), element-wise, other, high bits (>= 5), kernel (0 element-wise,
- * 1 direct single-gate sweep, 2 fused pass).  *nblocks gets the pass count;
- * at most max_blocks rows are written. */
+ * 1 direct single-gate sweep, 2 fused warp-tile or shared-memory pass,
+ * 3 float-float group pass, 4 float-float shape pass).  *nblocks gets the
+ * pass count; at most max_blocks rows are written. */
 int qf_plan_circuit(int n, int layout, int nops, const int* op_k, const int* op_axes, const double* op_mats,
                     int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
