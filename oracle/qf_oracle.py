@@ -40,6 +40,46 @@ def tensormul(gate, state, indices):
     return np.einsum(sub, g, s)
 
 
+# The reference's torch backend holds a complex tensor as a planar float64
+# stack [real, imag] of shape [2, 2, ..., 2] (quantumflow/backend/torchbk.py);
+# its tensormul is a permute -> matmul -> inverse permute on that layout,
+# multi-threaded on the CPU, and limited to 24 qubits (torchbk.py:60).
+def planar(state):
+    """Complex array -> the torch backend's planar float64 tensor [2, 2, ..., 2]."""
+    import torch
+    a = np.asarray(state, dtype=np.complex128)
+    n = int(round(np.log2(a.size)))
+    return torch.from_numpy(np.stack([a.real, a.imag]).reshape([2] + [2] * n).copy())
+
+
+def from_planar(t):
+    """The planar tensor back to a complex [2]*N numpy array."""
+    t = t.numpy()
+    return t[0] + 1j * t[1]
+
+
+def tensormul_planar(gate, tensor, indices):
+    """quantumflow/backend/torchbk.py:243-261 tensormul on planar tensors: the
+    state axes ``indices`` are permuted to the front (transpose, :180-186),
+    the tensor is reshaped to [2^K, 2^(N-K)] and multiplied by the gate with
+    four real matmuls (matmul, :198-205), then reshaped and permuted back.
+    ``gate`` is a complex (2^K, 2^K) array, ``tensor`` a planar state."""
+    import torch
+    K = len(indices)
+    N = tensor.dim() - 1
+    g = np.asarray(gate, dtype=np.complex128).reshape(2 ** K, 2 ** K)
+    g_re, g_im = torch.from_numpy(g.real.copy()), torch.from_numpy(g.imag.copy())
+    perm = list(indices) + [n for n in range(N) if n not in indices]
+    inv_perm = [int(i) for i in np.argsort(perm)]
+    re = tensor[0].permute(*perm).contiguous().view(2 ** K, 2 ** (N - K))
+    im = tensor[1].permute(*perm).contiguous().view(2 ** K, 2 ** (N - K))
+    new_re = g_re @ re - g_im @ im
+    new_im = g_re @ im + g_im @ re
+    shape = [2] * N
+    return torch.stack((new_re.view(shape).permute(*inv_perm).contiguous(),
+                        new_im.view(shape).permute(*inv_perm).contiguous()))
+
+
 def run_ops(state, ops):
     """Apply (matrix, axes) pairs in order (quantumflow/circuits.py:87-99)."""
     for m, axes in ops:

@@ -13,6 +13,16 @@ def test_tensormul_matches_reference(golden):
         np.testing.assert_allclose(out.reshape(-1), g[f"tm{c}_out"], rtol=0, atol=1e-12)
 
 
+def test_tensormul_planar_matches_reference(golden):
+    """The torch backend's permute + matmul tensormul (the multi-threaded CPU
+    baseline) against the same reference outputs."""
+    g = golden["tensormul"]
+    for c in range(int(g["tm_count"])):
+        st = g[f"tm{c}_state"]
+        out = orc.tensormul_planar(g[f"tm{c}_gate"], orc.planar(st), [int(i) for i in g[f"tm{c}_idx"]])
+        np.testing.assert_allclose(orc.from_planar(out).reshape(-1), g[f"tm{c}_out"], rtol=0, atol=1e-12)
+
+
 def test_kat_true_ket():
     # tests/test_circuits.py:43-60 circuit, KAT amplitudes from
     # tests/test_circuits.py:19-24 (referenceQVM)
