@@ -30,7 +30,6 @@ With ``torchrun --nproc-per-node N`` each rank runs an independent replica.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess

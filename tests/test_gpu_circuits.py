@@ -1,7 +1,5 @@
 """GPU parity: fused circuit execution against the reference's outputs, and
 size-independent properties at large N."""
-import math
-
 import numpy as np
 import pytest
 import torch
