@@ -208,6 +208,16 @@ class State:
     def memory(self) -> dict:
         return defaultdict(int, self._memory)
 
+    @property
+    def cbits(self) -> tuple:
+        """The classical bit addresses in memory, sorted (quantumflow/states.py:88-92)."""
+        return tuple(sorted(addr for addr in self._memory if getattr(addr, "dtype", None) == "BIT"))
+
+    @property
+    def cbit_nb(self) -> int:
+        """Number of classical bits in memory (quantumflow/states.py:95-97)."""
+        return len(self.cbits)
+
     def update(self, memory: Dict) -> "State":
         mem = self.memory
         mem.update(memory)

@@ -140,3 +140,34 @@ def test_upload_run_download_pipelined(dtype):
         ket.to_host(torch.empty(2 ** N + 1, dtype=cdt))
     with pytest.raises(ValueError):
         qf.upload_state(ins[0].cuda())
+
+
+def test_state_and_density_memory():
+    """Classical memory through updates, gates and channels
+    (tests/test_states.py:205-240 of the reference)."""
+    import quantumflow_gb300 as qf
+    ket0 = qf.zero_state(1)
+    assert ket0.memory == {}
+    ro = qf.Register("ro")
+    ket1 = ket0.update({ro[1]: 1})
+    assert ket0.memory == {}
+    assert ket1.memory == {ro[1]: 1}
+    assert ket1.cbit_nb == 1
+    assert ket1.cbits == (ro[1],)
+    ket2 = qf.H(0).run(ket1)
+    assert ket2.memory == ket1.memory
+    ket3 = ket2.update({ro[1]: 0, ro[0]: 0})
+    assert ket3.memory == {ro[0]: 0, ro[1]: 0}
+    assert ket3.cbits == (ro[0], ro[1])
+
+    rho0 = qf.zero_state(1).asdensity()
+    assert rho0.memory == {}
+    rho1 = rho0.update({ro[1]: 1})
+    assert rho0.memory == {}
+    assert rho1.memory == {ro[1]: 1}
+    assert rho1.cbit_nb == 1
+    assert rho1.cbits == (ro[1],)
+    rho2 = qf.H(0).aschannel().evolve(rho1)
+    assert rho2.memory == rho1.memory
+    rho3 = qf.X(0).evolve(rho1)
+    assert rho3.memory == rho1.memory

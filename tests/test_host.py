@@ -293,3 +293,19 @@ def test_backend_module_interface():
     missing = [n for n in required if not hasattr(qf.backend, n)]
     assert not missing, missing
     assert qf.backend.MAX_QUBITS >= 32
+
+
+def test_state_cbits_from_memory():
+    """State.cbits / cbit_nb (quantumflow/states.py:88-97): the sorted BIT
+    addresses of the classical memory (host only: they read the memory
+    dict, not the amplitudes)."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300.states import State
+    ro = qf.Register("ro")
+    re = qf.Register("re", "REAL")
+    st = State.__new__(State)
+    st._memory = {ro[1]: 1, re[0]: 0.5, ro[0]: 0}
+    assert st.cbits == (ro[0], ro[1])
+    assert st.cbit_nb == 2
+    st._memory = {}
+    assert st.cbits == () and st.cbit_nb == 0
