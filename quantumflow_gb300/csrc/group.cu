@@ -1,4 +1,5 @@
-// Group passes: fused passes whose dense gates touch at most four bits.
+// Float-float fused passes whose dense gates touch at most four bits:
+// shape kernels (k_shape, the default) and group kernels (k_group).
 //
 // The warp-tile kernel (k_warp) keeps bits 0..4 on the lanes and moves a
 // gate's lane bits into registers with shuffles; each of its decoded
@@ -6,9 +7,11 @@
 // so on passes with one or two dense gates and a row of CZ signs the
 // decoding and exchanges cost as much as the arithmetic.  Here a thread
 // holds all 2^G amplitudes that differ in the pass's gate bits, wherever
-// those bits are, so no amplitude leaves its thread: an op is decoded once
-// per 2^G amplitudes, dense gates run on register bits, and the lanes of a
-// warp fall on the lowest remaining bits (coalesced 16-byte accesses).
+// those bits are, so no amplitude leaves its thread: dense gates run on
+// register bits, and the lanes of a warp fall on the lowest remaining bits
+// (coalesced 16-byte accesses).  k_shape compiles one or two gates on fixed
+// register bits as straight-line code (the planner cuts passes to fit);
+// k_group interprets any op list, decoding each op once per 2^G amplitudes.
 //
 // Semantics are those of quantumflow/backend/numpybk.py:159-214 tensormul
 // applied in list order (quantumflow/circuits.py:87-99), as in every pass.
