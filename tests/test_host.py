@@ -309,3 +309,28 @@ def test_state_cbits_from_memory():
     assert st.cbit_nb == 2
     st._memory = {}
     assert st.cbits == () and st.cbit_nb == 0
+
+
+def test_bench_workload_definition():
+    """The benchmark's random-layer circuit: per layer a unitary 2x2 on every
+    qubit, then CZ on a perfect matching of all qubits; seeded and
+    deterministic; N=28 x 100 layers = 4200 gates."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    N, L = 28, 3
+    ops = bench.c2_circuit_ops(N, L, 2018)
+    again = bench.c2_circuit_ops(N, L, 2018)
+    assert len(ops) == L * (N + N // 2)
+    for layer in range(L):
+        chunk = ops[layer * (N + N // 2):(layer + 1) * (N + N // 2)]
+        ones, czs = chunk[:N], chunk[N:]
+        assert [qs for _, qs, _ in ones] == [(q,) for q in range(N)]
+        for kind, qs, u in ones:
+            assert kind == 1 and np.allclose(u @ u.conj().T, np.eye(2), atol=1e-12)
+        assert all(kind == 2 for kind, _, _ in czs)
+        assert sorted(q for _, qs, _ in czs for q in qs) == list(range(N))  # a perfect matching
+    for (k1, q1, u1), (k2, q2, u2) in zip(ops, again):
+        assert k1 == k2 and q1 == q2 and (u1 is None and u2 is None or np.array_equal(u1, u2))
+    assert len(bench.c2_circuit_ops(N, 100, 2018)) == 4200
