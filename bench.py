@@ -4,7 +4,10 @@ Workload (one step): a seeded random circuit on N qubits, L layers, each
 layer = a Haar-random U(2) on every qubit then CZ on a random perfect
 matching (N=28, L=100: 4200 gates), run by ``Circuit.run`` from |0...0>.
 The state (16 * 2^28 B = 4 GiB) is far larger than L2, so every pass streams
-from HBM; no flush is needed between steps.
+from HBM; no flush is needed between steps.  complex128 gates compute in
+the library's default arithmetic: FP64 storage with 64-bit integer
+fixed-point products (at least as accurate as FP64 arithmetic per pass);
+``--arith ff`` / ``fp64`` select float-float or native FP64.
 
 Reported (one JSON line on rank 0):
   value      effective gate GB/s = gates x (2 * 16 * 2^N bytes) / step time,
@@ -21,7 +24,8 @@ Reported (one JSON line on rank 0):
              against plain start + per-graph adjoint), the batched evaluation
              times and the single-instance adjoint gradient rate;
   cpu_baseline  the faster of two CPU oracle ports on a bounded sample of the
-             same circuit family at N=24: the reference numpy backend's
+             same circuit at N=28 (a walk over its first layer, one gate per
+             step, the reference arm's rule): the reference numpy backend's
              einsum (one thread) and its torch backend's permute + matmul
              (all threads); the other is reported under "other".
 
@@ -146,42 +150,48 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_oracle_rate(ops, N, budget_s=12.0):
-    """CPU oracle (numpy einsum restatement of the reference numpy backend)
-    on a prefix of the same circuit family at N qubits; returns
-    (gate GB/s, gates timed, seconds)."""
-    from oracle import qf_oracle as orc
-    st = orc.zero_state(N)
-    cz = orc.CZ()
-    t0 = time.perf_counter()
-    done = 0
-    for kind, qs, u in ops:
-        st = orc.tensormul(u if kind == 1 else cz, st, list(qs))
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return done * 2 * 16 * 2 ** N / dt / 1e9, done, dt
+def walk_sample(layer, step, per_step):
+    """Gates [per_step*step, per_step*(step+1)) of one layer of the circuit,
+    modulo its length: successive steps walk every qubit's U(2) and every CZ
+    of the layer, so a timed sample covers all axes (cheap low axes and
+    costly high ones alike) in the proportions of the workload."""
+    return [layer[(per_step * step + i) % len(layer)] for i in range(per_step)]
 
 
-def cpu_torch_rate(ops, N, budget_s=8.0):
-    """CPU oracle port of the reference's torch backend (permute + matmul
-    tensormul on planar float64 tensors, torch's intra-op threads) on a
-    prefix of the same circuit family at N qubits (the torch backend takes
-    at most 24); returns (gate GB/s, gates timed, seconds, threads)."""
+def cpu_sample_rates(N, seed, first_step, steps, per_step):
+    """The reference's two CPU paths as oracle ports on the same bounded
+    sample of the random-layer circuit at N qubits: its numpy backend's
+    tensormul (np.einsum, one thread; numpybk.py:159-214) and its torch
+    backend's permute + four-matmul tensormul (torch's intra-op threads, all
+    host cores; torchbk.py:243-261).  Step s applies walk_sample(layer 0, s,
+    per_step); steps first_step .. first_step+steps-1 are timed.  Returns one
+    record per port, the faster first."""
     import torch
     from oracle import qf_oracle as orc
-    st = orc.planar(orc.zero_state(N))
+    layer = c2_circuit_ops(N, 1, seed)
     cz = orc.CZ()
-    t0 = time.perf_counter()
-    done = 0
-    for kind, qs, u in ops:
-        st = orc.tensormul_planar(u if kind == 1 else cz, st, list(qs))
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return done * 2 * 16 * 2 ** N / dt / 1e9, done, dt, torch.get_num_threads()
+    gate_bytes = 2 * 16 * 2 ** N
+    recs = []
+    for name, mul, st, cores in (
+            ("numpy-backend einsum port", orc.tensormul, orc.zero_state(N), 1),
+            ("torch-backend permute+matmul port (planar float64)", orc.tensormul_planar,
+             orc.planar(orc.zero_state(N)), torch.get_num_threads())):
+        t = 0.0
+        for s in range(first_step, first_step + steps):
+            sample = walk_sample(layer, s, per_step)
+            t0 = time.perf_counter()
+            for kind, qs, u in sample:
+                st = mul(u if kind == 1 else cz, st, list(qs))
+            t += time.perf_counter() - t0
+        del st
+        recs.append({"value": steps * per_step * gate_bytes / t / 1e9, "unit": "GB/s", "cores": cores,
+                     "kind": "port", "ms_per_step": t / steps * 1e3,
+                     "sample": f"{name}, N={N} complex128, steps {first_step}..{first_step + steps - 1} of a "
+                               f"walk over layer 0 of the random-layer circuit ({per_step} gates per step: "
+                               f"gates [{per_step}s, {per_step}s+{per_step}) mod {len(layer)}), "
+                               f"{t:.1f} s, {cores} thread(s)"})
+    recs.sort(key=lambda r: -r["value"])
+    return recs
 
 
 def qaoa_time_to_ratio(args):
@@ -276,51 +286,24 @@ def run_reference(args, rank, world):
     """Reference arm: the reference's two CPU paths as oracle ports (the
     reference is pure Python): its numpy backend's tensormul (np.einsum, one
     thread) and its torch backend's permute + matmul tensormul (torch's
-    intra-op threads), each on the same bounded sample; the faster is
-    reported, the other under "other"."""
+    intra-op threads), each on the same bounded sample (cpu_sample_rates:
+    W untimed steps of the walk over the first layer, then K timed ones);
+    the faster is reported, the other under "other"."""
     if rank != 0:
         return
-    import torch
     N = args.ref_n
-    ops = c2_circuit_ops(N, 1, args.seed)
-    from oracle import qf_oracle as orc
     per_step = args.ref_gates
-    cz = orc.CZ()
-
-    def timed(mul, st):
-        def step(st):
-            for kind, qs, u in ops[:per_step]:
-                st = mul(u if kind == 1 else cz, st, list(qs))
-            return st
-        for w in range(args.warmup):
-            st = step(st)
-        t0 = time.perf_counter()
-        for s in range(args.steps):
-            st = step(st)
-        return (time.perf_counter() - t0) / args.steps
-
-    dt_np = timed(orc.tensormul, orc.zero_state(N))
-    dt_torch = timed(orc.tensormul_planar, orc.planar(orc.zero_state(N)))
-    threads = torch.get_num_threads()
-    ports = [
-        {"value": per_step * 2 * 16 * 2 ** N / dt_np / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
-         "ms_per_step": dt_np * 1e3,
-         "sample": f"numpy-backend einsum port, N={N} complex128, {per_step} gates of layer 0 of the "
-                   f"random-layer circuit per step, single thread (np.einsum)"},
-        {"value": per_step * 2 * 16 * 2 ** N / dt_torch / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
-         "ms_per_step": dt_torch * 1e3,
-         "sample": f"torch-backend permute+matmul port, N={N} complex128 (planar float64), {per_step} gates "
-                   f"of layer 0 of the random-layer circuit per step, {threads} threads"},
-    ]
-    ports.sort(key=lambda p: -p["value"])
-    best, other = ports
+    from oracle import qf_oracle as orc  # noqa: F401  (the ports live there)
+    # warm-up: the first W steps of the walk, untimed; then K timed steps
+    cpu_sample_rates(N, args.seed, 0, args.warmup, per_step)
+    best, other = cpu_sample_rates(N, args.seed, args.warmup, args.steps, per_step)
     value, dt, sample = best["value"], best["ms_per_step"] * 1e-3, best["sample"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64)", "data": "synthetic",
         "config": {"workload": f"random-layer circuit N={N} (Haar U(2) per qubit + CZ matching), "
-                               f"bounded sample of {per_step} gates per step"},
+                               f"bounded sample of {per_step} gates per step walking layer 0"},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": best["cores"], "kind": "port", "sample": sample,
                          "other": other},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -337,7 +320,8 @@ def main():
     ap.add_argument("--n", type=int, default=28)
     ap.add_argument("--layers", type=int, default=100)
     ap.add_argument("--dtype", default="complex128", choices=["complex128", "complex64"])
-    ap.add_argument("--arith", default=None, choices=["ff", "fp64"])
+    ap.add_argument("--arith", default=None, choices=["fx", "ff", "fp64"],
+                    help="complex128 arithmetic (default: the library's, fixed point)")
     ap.add_argument("--fusion", type=int, default=0, help="0 = library default per element type")
     ap.add_argument("--seed", type=int, default=2018)
     ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
@@ -349,8 +333,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-n", type=int, default=28)
-    ap.add_argument("--ref-gates", type=int, default=3)
-    ap.add_argument("--cpu-n", type=int, default=24)
+    ap.add_argument("--ref-gates", type=int, default=1, help="gates per reference-arm step (CPU sample)")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed steps of the cpu_baseline sample")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -498,22 +482,11 @@ def main():
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        # both of the reference's CPU paths, as oracle ports: the numpy
-        # backend's einsum (one thread) and the torch backend's permute +
-        # matmul (all intra-op threads); the faster is the baseline
-        cpu_ops = c2_circuit_ops(args.cpu_n, 1, args.seed)
-        v, done, dt = cpu_oracle_rate(cpu_ops, args.cpu_n)
-        numpy_port = {"value": v, "unit": "GB/s", "cores": 1, "kind": "port",
-                      "sample": f"numpy-backend einsum port, N={args.cpu_n} complex128, first {done} gates of "
-                                f"the random-layer circuit ({dt:.1f} s, single thread)"}
-        v, done, dt, threads = cpu_torch_rate(cpu_ops, args.cpu_n)
-        torch_port = {"value": v, "unit": "GB/s", "cores": threads, "kind": "port",
-                      "sample": f"torch-backend permute+matmul port, N={args.cpu_n} complex128 (planar "
-                                f"float64), first {done} gates of the random-layer circuit ({dt:.1f} s, "
-                                f"{threads} threads)"}
-        cpu, other = (numpy_port, torch_port) if numpy_port["value"] >= torch_port["value"] else \
-            (torch_port, numpy_port)
-        cpu = dict(cpu, other=other)
+        # both of the reference's CPU paths, as oracle ports, on the sample
+        # rule of the reference arm (a walk over the first layer at the
+        # workload's N); the faster is the baseline
+        best, other = cpu_sample_rates(N, args.seed, 0, args.cpu_steps, args.ref_gates)
+        cpu = dict(best, other=other)
 
     if rank == 0:
         arith = qf.config.C128_ARITHMETIC if args.dtype == "complex128" else "fp32"
@@ -521,7 +494,9 @@ def main():
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"ff": "c128 (float-float arithmetic)", "fp64": "c128 (FP64)",
+            "dtype": {"fx": "c128 (FP64 storage; int64 fixed-point gate arithmetic, >= 55-bit, "
+                            "one FP64 rounding per pass)",
+                      "ff": "c128 (float-float arithmetic)", "fp64": "c128 (FP64)",
                       "fp32": "c64 (FP32)"}[arith],
             "data": "synthetic",
             "config": {"workload": f"random-layer circuit N={N}, {args.layers} layers x (Haar U(2) on "

@@ -24,6 +24,15 @@
  *   QF_LAYOUT_FF    complex128 value held as float-float pairs
  *                   (re_hi, re_lo, im_hi, im_lo), 48-bit significand,
  *                   float-float math on the FP32 pipes            16
+ *   QF_LAYOUT_FX    complex128 (double re, double im), the same bytes as
+ *                   QF_LAYOUT_C128; gates computed in 64-bit integer
+ *                   fixed point (each thread's amplitude group shares one
+ *                   exponent, >= 55 significant bits relative to the
+ *                   group's largest part, one FP64 rounding per pass).
+ *                   Unitary gates only take this arithmetic; other gates,
+ *                   and every entry point other than qf_apply_gate /
+ *                   qf_run_circuit / qf_plan_circuit, treat the buffer as
+ *                   QF_LAYOUT_C128 (native FP64)                  16
  */
 #ifndef QF_GB300_H
 #define QF_GB300_H
@@ -40,6 +49,7 @@ extern "C" {
 #define QF_LAYOUT_C64 0
 #define QF_LAYOUT_C128 1
 #define QF_LAYOUT_FF 2
+#define QF_LAYOUT_FX 3
 
 #define QF_OK 0
 #define QF_ERR_INVALID_ARGUMENT 1 /* bad qubit index, k, n, null pointer, ... */
@@ -53,6 +63,7 @@ extern "C" {
 
 #define QF_MAX_QUBITS 34
 #define QF_MAX_GATE_QUBITS 5
+#define QF_MAX_DENSE_QUBITS 12
 
 /* ------------------------------------------------------------ utilities -- */
 int qf_abi_version(void);
@@ -80,7 +91,11 @@ size_t qf_reduce_workspace_bytes(int n);
 #define QF_KERNEL_WARP_TILE 5
 #define QF_KERNEL_GROUP 6
 #define QF_KERNEL_SHAPE 7
-#define QF_KERNEL_CLASSES 8
+#define QF_KERNEL_FX_DENSE1 8      /* fixed-point 2x2 sweep (QF_LAYOUT_FX)        */
+#define QF_KERNEL_FX_DENSE2 9      /* fixed-point 4x4 sweep                       */
+#define QF_KERNEL_FX_GROUP 10      /* fixed-point fused pass on a register group  */
+#define QF_KERNEL_FX_ELEMENTWISE 11 /* fixed-point pass of element-wise ops only  */
+#define QF_KERNEL_CLASSES 12
 int qf_timing_enable(int on);
 /* Fused-pass kernel selection (diagnostics and tests; no reference
  * counterpart), process-wide: 0 = default (float-float group passes --
@@ -134,6 +149,17 @@ int qf_scale(void* psi, int n, int layout, double scale, void* stream);
  * k = 1..QF_MAX_GATE_QUBITS, matrix = 2*4^k interleaved doubles (host). */
 int qf_apply_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
                   const double* matrix, void* stream);
+
+/* psi_out = gate (.) psi_in for a dense gate on k = 1..QF_MAX_DENSE_QUBITS
+ * axes whose matrix is in DEVICE memory (2 * 4^k interleaved doubles,
+ * row-major, the convention of qf_apply_gate; 16-byte aligned).  Replaces
+ * quantumflow/backend/numpybk.py:159-214 tensormul for gates wider than
+ * qf_apply_gate takes (Gate.__matmul__, quantumflow/ops.py:187-198;
+ * Circuit.asgate, quantumflow/circuits.py:111-118).  psi_out may equal
+ * psi_in.  complex64 computes in FP32, the complex128 layouts in FP64 (a
+ * float-float state is converted to complex128 in psi_out and back). */
+int qf_apply_dense_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
+                        const double* matrix, void* stream);
 
 /* Apply nops gates in order with gate fusion.  Replaces the per-gate loop of
  * quantumflow/circuits.py:87-99 Circuit.run.  Gate i acts on op_k[i] axes
@@ -275,9 +301,11 @@ int qf_expectation_cuts(const void* psi, int n, int layout, const uint16_t* cuts
  * in a fixed array compiled into the library: QF_NOALLOC_MAX_PARTIALS block
  * partials (32 KiB per GPU, held until exit), enough for every n up to
  * QF_MAX_QUBITS (larger n: QF_ERR_TOO_LARGE).  All calls share that array,
- * so calls whose kernels overlap on the GPU race; serialise them.  The first
- * call on a device looks up the array's device address with that device
- * current; make that call before any stream capture. */
+ * so calls whose kernels overlap on the GPU race; serialise them.  A call
+ * whose stream is not capturing looks up the array's device address with
+ * the calling device current (so the address survives a device reset); a
+ * call made during stream capture reuses the last address found on that
+ * device, so make one call per device before any stream capture. */
 #define QF_NOALLOC_MAX_PARTIALS 2048
 int qf_expectation_cuts_noalloc(const void* psi, int n, int layout, const uint16_t* cuts, double* out,
                                 void* stream);

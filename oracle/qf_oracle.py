@@ -17,15 +17,17 @@ EINSUM_SUBSCRIPTS = "abcdefghijklmnopqrstuvwxyzABCDEFGHIJKLMNOPQRSTUVWXYZ"
 
 
 # ------------------------------------------------------------ core ---------
-def tensormul(gate, state, indices):
+def tensormul(gate, state, indices, dtype=np.complex128):
     """Contract a K-qubit gate with an N-axis tensor on ``indices``.
 
     Restates quantumflow/backend/numpybk.py:159-214: the gate's bra axes are
     summed against the state axes ``indices`` and its ket axes written back
     at the same positions (out of place).  ``gate`` is (2^K, 2^K) or
-    [2]*2K; ``state`` is [2]*N or flat."""
-    gate = np.asarray(gate, dtype=np.complex128)
-    state = np.asarray(state, dtype=np.complex128)
+    [2]*2K; ``state`` is [2]*N or flat.  ``dtype`` np.clongdouble evaluates
+    the same contraction in the host's extended precision (an accuracy
+    yardstick for the tests; the reference computes in complex128)."""
+    gate = np.asarray(gate, dtype=dtype)
+    state = np.asarray(state, dtype=dtype)
     K = len(indices)
     N = int(round(np.log2(state.size)))
     g = gate.reshape([2] * (2 * K))
@@ -80,10 +82,10 @@ def tensormul_planar(gate, tensor, indices):
                         new_im.view(shape).permute(*inv_perm).contiguous()))
 
 
-def run_ops(state, ops):
+def run_ops(state, ops, dtype=np.complex128):
     """Apply (matrix, axes) pairs in order (quantumflow/circuits.py:87-99)."""
     for m, axes in ops:
-        state = tensormul(m, state, list(axes))
+        state = tensormul(m, state, list(axes), dtype)
     return state
 
 
@@ -310,6 +312,22 @@ def qaoa_fd_gradient(n, edges, p, beta, gamma, h=1e-6, weights=None, node_weight
 
 
 # --------------------------------------------------- random-layer circuit --
+def layer_family_ops(umats, pairs):
+    """The random-layer family (a U(2) on every qubit, then CZ on each pair of
+    a perfect matching, per layer) from its stored gates: umats [L*N, 2, 2]
+    layer-major, pairs [L, N/2, 2]."""
+    L, half = pairs.shape[0], pairs.shape[1]
+    N = umats.shape[0] // L
+    out = []
+    for layer in range(L):
+        for q in range(N):
+            out.append((umats[layer * N + q], (q,)))
+        for a, b in pairs[layer]:
+            out.append((CZ(), (int(a), int(b))))
+    assert half == N // 2
+    return out
+
+
 def cz_layer_ops(ops_array, umats):
     """Decode the (kind, q0, q1) op table of the golden random-layer circuits
     into (matrix, axes) pairs."""

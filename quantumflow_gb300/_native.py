@@ -16,6 +16,9 @@ LIBPATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libq
 LAYOUT_C64 = 0
 LAYOUT_C128 = 1
 LAYOUT_FF = 2
+LAYOUT_FX = 3  # complex128 bytes (as LAYOUT_C128); gates in 64-bit fixed point
+MAX_GATE_QUBITS = 5    # qf_apply_gate / qf_run_circuit (host matrices)
+MAX_DENSE_QUBITS = 12  # qf_apply_dense_gate (device matrix)
 
 STATUS = {
     0: "ok",
@@ -73,6 +76,7 @@ SIGNATURES = {
     "qf_convert": (_c_int, [_vp, _c_int, _vp, _c_int, _c_int, _vp]),
     "qf_scale": (_c_int, [_vp, _c_int, _c_int, _c_dbl, _vp]),
     "qf_apply_gate": (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _ip, _dp, _vp]),
+    "qf_apply_dense_gate": (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _ip, _vp, _vp]),
     "qf_run_circuit": (_c_int, [_vp, _vp, _c_int, _c_int, _c_int, _ip, _ip, _dp, _c_int, _ip, _vp]),
     "qf_cut_values": (_c_int, [_vp, _c_int, _c_int, _ip, _vp]),
     "qf_cut_values_weighted": (_c_int, [_vp, _c_int, _c_int, _ip, _dp, _vp]),
@@ -156,7 +160,8 @@ def device_error(stream=None):
     return flags.value
 
 
-KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile", "group", "shape")
+KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile", "group", "shape",
+                  "fx_dense1", "fx_dense2", "fx_group", "fx_elementwise")
 
 
 def timing_enable(on=True):

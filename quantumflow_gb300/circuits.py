@@ -14,7 +14,7 @@ from . import config
 from .gates import identity_gate
 from .ops import Gate, Operation
 from .qubits import Qubits
-from .states import Buffer, State, compute_layout, zero_state
+from .states import Buffer, State, compute_layout, gate_layout, zero_state
 
 __all__ = ["Circuit", "count_operations", "map_gate", "reversal_circuit", "qft_circuit", "control_circuit",
            "ccnot_circuit", "zyz_circuit", "phase_estimation_circuit", "addition_circuit", "ghz_circuit"]
@@ -94,12 +94,13 @@ class Circuit(Operation):
         if fresh:
             ket = zero_state(self.qubits)
         flat = self.gates()
-        if any(not isinstance(g, Gate) for g in flat):
+        if any(not isinstance(g, Gate) or g.qubit_nb > nat.MAX_GATE_QUBITS for g in flat):
             # mixed operations: each run of consecutive gates is one fused
-            # launch, other operations run on their own in between
+            # launch, other operations (and gates wider than the fused
+            # engine takes) run on their own in between
             pending = []
             for elem in flat:
-                if isinstance(elem, Gate):
+                if isinstance(elem, Gate) and elem.qubit_nb <= nat.MAX_GATE_QUBITS:
                     pending.append(elem)
                     continue
                 if pending:
@@ -113,7 +114,7 @@ class Circuit(Operation):
         src = ket.buffer.compute()
         out = src if (fresh or src is not ket.buffer) else src.empty_like()
         passes = (nat.ctypes.c_int * 1)()
-        nat.call("qf_run_circuit", nat.ptr(src.data), nat.ptr(out.data), src.n, src.layout, nops,
+        nat.call("qf_run_circuit", nat.ptr(src.data), nat.ptr(out.data), src.n, gate_layout(src), nops,
                  op_k.ctypes.data_as(nat._ip), op_axes.ctypes.data_as(nat._ip),
                  op_mats.ctypes.data_as(nat._dp), int(fusion_k), passes, nat.stream_handle(src.device))
         self.last_passes = passes[0]

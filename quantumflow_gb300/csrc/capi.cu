@@ -17,6 +17,8 @@ extern int g_merge_gates;
 extern int g_group_kernel;
 extern int g_shape_max_bits;
 int read_clear_device_error(int* flags, cudaStream_t stream);
+int apply_dense_gate(const void* in, void* out, int n, int layout, int k, const int* bits, const double* mat,
+                     cudaStream_t stream);
 int qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p, const double* beta,
                const double* gamma, const double* node_theta, int fusion_k, cudaStream_t stream);
 size_t qaoa_grad_workspace_bytes(int n, int p, int layout);
@@ -40,7 +42,11 @@ using namespace qf;
 
 namespace {
 
-bool valid_layout(int layout) { return layout == C64 || layout == C128 || layout == FF; }
+bool valid_layout(int layout) { return layout == C64 || layout == C128 || layout == FF || layout == FX; }
+
+// Storage layout of a buffer: QF_LAYOUT_FX holds complex128 values in the
+// QF_LAYOUT_C128 bytes; only the gate engine computes differently on it.
+int st(int layout) { return layout == FX ? C128 : layout; }
 
 int check_state(const void* p, int n, int layout) {
   if (!valid_layout(layout)) return QF_ERR_LAYOUT;
@@ -142,13 +148,13 @@ int qf_fill_basis(void* psi, int n, int layout, int64_t index, void* stream) {
   int rc = check_state(psi, n, layout);
   if (rc) return rc;
   if (index < 0 || index >= (int64_t(1) << n)) return QF_ERR_INVALID_ARGUMENT;
-  return fill_basis(psi, n, layout, index, as_stream(stream));
+  return fill_basis(psi, n, st(layout), index, as_stream(stream));
 }
 
 int qf_fill_uniform(void* psi, int n, int layout, void* stream) {
   int rc = check_state(psi, n, layout);
   if (rc) return rc;
-  return fill_uniform(psi, n, layout, as_stream(stream));
+  return fill_uniform(psi, n, st(layout), as_stream(stream));
 }
 
 int qf_convert(const void* src, int src_layout, void* dst, int dst_layout, int n, void* stream) {
@@ -157,13 +163,13 @@ int qf_convert(const void* src, int src_layout, void* dst, int dst_layout, int n
   rc = check_state(dst, n, dst_layout);
   if (rc) return rc;
   if (src == dst) return QF_ERR_INVALID_ARGUMENT;
-  return convert(src, src_layout, dst, dst_layout, n, as_stream(stream));
+  return convert(src, st(src_layout), dst, st(dst_layout), n, as_stream(stream));
 }
 
 int qf_scale(void* psi, int n, int layout, double s, void* stream) {
   int rc = check_state(psi, n, layout);
   if (rc) return rc;
-  return scale(psi, n, layout, s, as_stream(stream));
+  return scale(psi, n, st(layout), s, as_stream(stream));
 }
 
 int qf_apply_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
@@ -180,6 +186,25 @@ int qf_apply_gate(const void* psi_in, void* psi_out, int n, int layout, int k, c
   rc = classify_op(k, bits, matrix, ops[0]);
   if (rc) return rc;
   return run_ops(psi_in, psi_out, n, layout, ops, 1, as_stream(stream), nullptr);
+}
+
+int qf_apply_dense_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
+                        const double* matrix, void* stream) {
+  int rc = check_state(psi_in, n, layout);
+  if (rc) return rc;
+  rc = check_state(psi_out, n, layout);
+  if (rc) return rc;
+  if (matrix == nullptr || axes == nullptr || k < 1 || k > n) return QF_ERR_INVALID_ARGUMENT;
+  if (k > QF_MAX_DENSE_QUBITS) return QF_ERR_NOT_SUPPORTED;
+  if ((reinterpret_cast<uintptr_t>(matrix) & 15u) != 0) return QF_ERR_ALIGNMENT;
+  int bits[QF_MAX_DENSE_QUBITS];
+  for (int i = 0; i < k; ++i) {
+    if (axes[i] < 0 || axes[i] >= n) return QF_ERR_INVALID_ARGUMENT;
+    for (int j = 0; j < i; ++j)
+      if (axes[j] == axes[i]) return QF_ERR_INVALID_ARGUMENT;
+    bits[i] = n - 1 - axes[i];
+  }
+  return apply_dense_gate(psi_in, psi_out, n, layout, k, bits, matrix, as_stream(stream));
 }
 
 int qf_run_circuit(const void* psi_in, void* psi_out, int n, int layout, int nops, const int* op_k,
@@ -257,7 +282,7 @@ int qf_qaoa_state(void* psi, int n, int layout, const uint16_t* cuts, int nedges
   if (cuts == nullptr || p < 0 || nedges < 0) return QF_ERR_INVALID_ARGUMENT;
   if (p > 0 && (beta == nullptr || gamma == nullptr)) return QF_ERR_INVALID_ARGUMENT;
   if (nedges + 1 > 1024) return QF_ERR_TOO_LARGE;
-  return qaoa_state(psi, n, layout, cuts, nedges, p, beta, gamma, node_theta, fusion_k,
+  return qaoa_state(psi, n, st(layout), cuts, nedges, p, beta, gamma, node_theta, fusion_k,
                     as_stream(stream));
 }
 
@@ -315,7 +340,7 @@ int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, int n
 
 size_t qf_qaoa_grad_workspace_bytes(int n, int p, int layout) {
   if (n < 1 || n > QF_MAX_QUBITS || p < 0 || !valid_layout(layout)) return 0;
-  return qaoa_grad_workspace_bytes(n, p, layout);
+  return qaoa_grad_workspace_bytes(n, p, st(layout));
 }
 
 int qf_qaoa_expectation_grad(void* psi, int n, int layout, const uint16_t* cuts, int nedges, int p,
@@ -327,6 +352,7 @@ int qf_qaoa_expectation_grad(void* psi, int n, int layout, const uint16_t* cuts,
   if (cuts == nullptr || out == nullptr || p < 0 || nedges < 0) return QF_ERR_INVALID_ARGUMENT;
   if (p > 0 && (beta == nullptr || gamma == nullptr)) return QF_ERR_INVALID_ARGUMENT;
   if (nedges + 1 > 1024 || 2 * p + 1 > 64) return QF_ERR_TOO_LARGE;
+  layout = st(layout);
   rc = check_ws(workspace, workspace_bytes, qaoa_grad_workspace_bytes(n, p, layout));
   if (rc) return rc;
   if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
@@ -343,7 +369,7 @@ int qf_expectation_cuts(const void* psi, int n, int layout, const uint16_t* cuts
   if (cuts == nullptr || out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
   if (rc) return rc;
-  return reduce_diag(psi, n, layout, 1, cuts, nullptr, out, reinterpret_cast<double*>(workspace),
+  return reduce_diag(psi, n, st(layout), 1, cuts, nullptr, out, reinterpret_cast<double*>(workspace),
                      as_stream(stream));
 }
 
@@ -354,7 +380,7 @@ int qf_expectation_diag(const void* psi, int n, int layout, const double* diag, 
   if (diag == nullptr || out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
   if (rc) return rc;
-  return reduce_diag(psi, n, layout, 2, nullptr, diag, out, reinterpret_cast<double*>(workspace),
+  return reduce_diag(psi, n, st(layout), 2, nullptr, diag, out, reinterpret_cast<double*>(workspace),
                      as_stream(stream));
 }
 
@@ -365,7 +391,7 @@ int qf_qubit_probabilities(const void* psi, int n, int layout, int axis, double*
   if (out == nullptr || axis < 0 || axis >= n) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
   if (rc) return rc;
-  return reduce_bit(psi, n, layout, n - 1 - axis, out, reinterpret_cast<double*>(workspace), as_stream(stream));
+  return reduce_bit(psi, n, st(layout), n - 1 - axis, out, reinterpret_cast<double*>(workspace), as_stream(stream));
 }
 
 int qf_norm2(const void* psi, int n, int layout, double* out, void* workspace, size_t workspace_bytes,
@@ -375,7 +401,7 @@ int qf_norm2(const void* psi, int n, int layout, double* out, void* workspace, s
   if (out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
   if (rc) return rc;
-  return reduce_diag(psi, n, layout, 0, nullptr, nullptr, out, reinterpret_cast<double*>(workspace),
+  return reduce_diag(psi, n, st(layout), 0, nullptr, nullptr, out, reinterpret_cast<double*>(workspace),
                      as_stream(stream));
 }
 
@@ -388,14 +414,14 @@ int qf_inner(const void* a, const void* b, int n, int layout, double* out, void*
   if (out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, qf_reduce_workspace_bytes(n));
   if (rc) return rc;
-  return reduce_inner(a, b, n, layout, out, reinterpret_cast<double*>(workspace), as_stream(stream));
+  return reduce_inner(a, b, n, st(layout), out, reinterpret_cast<double*>(workspace), as_stream(stream));
 }
 
 int qf_probabilities(const void* psi, int n, int layout, double* probs, void* stream) {
   int rc = check_state(psi, n, layout);
   if (rc) return rc;
   if (probs == nullptr) return QF_ERR_INVALID_ARGUMENT;
-  return probabilities(psi, n, layout, probs, as_stream(stream));
+  return probabilities(psi, n, st(layout), probs, as_stream(stream));
 }
 
 int qf_sample(const void* psi, int n, int layout, int64_t trials, uint64_t seed, int64_t* counts,
@@ -405,7 +431,7 @@ int qf_sample(const void* psi, int n, int layout, int64_t trials, uint64_t seed,
   if (counts == nullptr || trials < 0) return QF_ERR_INVALID_ARGUMENT;
   rc = check_ws(workspace, workspace_bytes, sample_workspace_bytes(n));
   if (rc) return rc;
-  return sample(psi, n, layout, trials, seed, counts, workspace, as_stream(stream));
+  return sample(psi, n, st(layout), trials, seed, counts, workspace, as_stream(stream));
 }
 
 }  // extern "C"

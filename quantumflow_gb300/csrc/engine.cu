@@ -932,27 +932,22 @@ cudaEvent_t pooled_event() {
 }
 }  // namespace
 
-struct LaunchTimer {
-  bool on = false;
-  TimedLaunch t{};
-  cudaStream_t s = nullptr;
-  LaunchTimer(int kind, cudaStream_t stream) {
-    std::lock_guard<std::mutex> g(g_timing_mu);
-    if (!g_timing_on) return;
-    on = true;
-    s = stream;
-    t.kind = kind;
-    t.start = pooled_event();
-    t.stop = pooled_event();
-    cudaEventRecord(t.start, s);
-  }
-  ~LaunchTimer() {
-    if (!on) return;
-    cudaEventRecord(t.stop, s);
-    std::lock_guard<std::mutex> g(g_timing_mu);
-    g_timed.push_back(t);
-  }
-};
+LaunchTimer::LaunchTimer(int k, cudaStream_t stream) {
+  std::lock_guard<std::mutex> g(g_timing_mu);
+  if (!g_timing_on) return;
+  on = true;
+  s = stream;
+  kind = k;
+  start = pooled_event();
+  stop = pooled_event();
+  cudaEventRecord(start, s);
+}
+LaunchTimer::~LaunchTimer() {
+  if (!on) return;
+  cudaEventRecord(stop, s);
+  std::lock_guard<std::mutex> g(g_timing_mu);
+  g_timed.push_back(TimedLaunch{kind, start, stop});
+}
 
 int timing_enable(int on) {
   std::lock_guard<std::mutex> g(g_timing_mu);
@@ -1992,6 +1987,7 @@ static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int l
 // 4 shape pass).
 int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks,
                int* nblocks) {
+  if (layout == FX) return fx_plan_stats(n, ops, fusion_k, stats, max_blocks, nblocks);
   std::vector<PlanBlock> blocks = plan_blocks(ops, n, layout, fusion_k);
   *nblocks = (int)blocks.size();
   for (int b = 0; b < (int)blocks.size() && b < max_blocks; ++b) {
@@ -2026,6 +2022,7 @@ int plan_stats(int n, int layout, std::vector<HostOp>& ops, int fusion_k, int32_
 
 int run_ops(const void* in, void* out, int n, int layout, std::vector<HostOp>& ops, int fusion_k,
             cudaStream_t stream, int* passes_out) {
+  if (layout == FX) return fx_run_ops(in, out, n, ops, fusion_k, stream, passes_out);
   const int Lmin = 5;
   std::vector<PlanBlock> blocks = plan_blocks(ops, n, layout, fusion_k);
   int passes = 0;

@@ -234,6 +234,29 @@ int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::
 int shape_launch(const ShapeParams& P, cudaStream_t stream);
 extern int g_shape_max_bits;  // qf_set_shape_bits (0: no shape passes, blocks stay whole)
 
+// While qf_timing_enable is on, a CUDA event pair brackets the launches made
+// during this object's lifetime on `stream`, summed under kernel class `kind`.
+struct LaunchTimer {
+  bool on = false;
+  int kind = 0;
+  cudaEvent_t start = nullptr, stop = nullptr;
+  cudaStream_t s = nullptr;
+  LaunchTimer(int kind, cudaStream_t stream);
+  ~LaunchTimer();
+  LaunchTimer(const LaunchTimer&) = delete;
+  LaunchTimer& operator=(const LaunchTimer&) = delete;
+};
+
+// Consecutive gates multiplied into blocks of at most two qubits (host).
+void merge_ops(std::vector<HostOp>& ops, int n);
+extern int g_merge_gates;
+
+// Passes of complex128 states in 64-bit integer fixed-point arithmetic
+// (fxengine.cu); ops the fixed-point kernels do not take run in native FP64.
+int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int fusion_k, cudaStream_t stream,
+               int* passes_out);
+int fx_plan_stats(int n, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
+
 int device_sm_count();
 int timing_enable(int on);
 int timing_collect(double* ms, int64_t* counts, int nkinds);

@@ -1,0 +1,634 @@
+// Gate passes on complex128 states in 64-bit integer fixed-point arithmetic
+// (QF_LAYOUT_FX; the arithmetic is described in fx.cuh).
+//
+// Semantics are those of quantumflow/backend/numpybk.py:159-214 tensormul
+// applied in list order (quantumflow/circuits.py:87-99): the state is swept
+// once per pass, each pass applying a run of gates whose dense qubits fit one
+// thread's register group.
+//
+// Kernels:
+//   k_fxdense1  one 2x2 gate on any bit (a thread holds two amplitude pairs)
+//   k_fxdense2  one 4x4 gate on any two bits (a thread holds one quad)
+//   k_fxgroup<G> an op list on a group of 2^G amplitudes per thread (the
+//               pass's dense gate bits, G <= 4), with sign (CZ-like),
+//               diagonal, phase and cut-table ops; G = 0 is a pass of
+//               element-wise ops only
+// Each kernel converts the amplitudes it holds to fixed point once, applies
+// its gates, and rounds to FP64 once.
+#include <algorithm>
+#include <cstring>
+
+#include "engine.cuh"
+#include "fx.cuh"
+
+namespace qf {
+
+// ------------------------------------------------------------- device ----
+template <int R>
+QF_D int fx_group_exp(const double2 (&v)[R]) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    m = max(m, fx_hiword(v[r].x) & 0x7fffffffu);
+    m = max(m, fx_hiword(v[r].y) & 0x7fffffffu);
+  }
+  return static_cast<int>(m >> 20);
+}
+
+template <int M>
+QF_D FxAmp fx_load_amp(double2 v, int E) {
+  FxAmp a;
+  fx_in<M>(v.x, E, a.rh, a.rl);
+  fx_in<M>(v.y, E, a.ih, a.il);
+  return a;
+}
+template <int M>
+QF_D double2 fx_store_amp(const FxAmp& a, int E) {
+  return make_double2(fx_out<M>(fx_t_of(a.rh, a.rl), E), fx_out<M>(fx_t_of(a.ih, a.il), E));
+}
+// flip the FP64 sign of both parts (a pending CZ-like sign at store time)
+QF_D double2 fx_flip(double2 v, bool neg) {
+  if (neg) {
+    v.x = -v.x;
+    v.y = -v.y;
+  }
+  return v;
+}
+
+struct FxCoef4 {
+  FxC c[4];
+};
+struct FxCoef16 {
+  FxC c[16];
+};
+
+// 2x2 gate on bit b: each thread takes pairs t and t + nthr per iteration
+template <typename IT>
+__global__ void __launch_bounds__(256) k_fxdense1(const double2* __restrict__ in, double2* out, IT npairs, int b,
+                                                  const __grid_constant__ FxCoef4 u) {
+  constexpr int M = 57;
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  const IT bit = IT(1) << b;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += 2 * nthr) {
+    const IT t2 = t + nthr;
+    const bool has2 = t2 < npairs;
+    const IT i0 = insert0(t, b);
+    const IT j0 = has2 ? insert0(t2, b) : i0;
+    double2 a[2] = {in[i0], in[i0 | bit]};
+    double2 c[2];
+    if (has2) {
+      c[0] = in[j0];
+      c[1] = in[j0 | bit];
+    }
+    {
+      const int E = fx_group_exp<2>(a);
+      FxAmp f[2] = {fx_load_amp<M>(a[0], E), fx_load_amp<M>(a[1], E)};
+      int64_t tr, ti;
+      fx_cdot<2>(&u.c[0], f, tr, ti);
+      out[i0] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      fx_cdot<2>(&u.c[2], f, tr, ti);
+      out[i0 | bit] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+    }
+    if (has2) {
+      const int E = fx_group_exp<2>(c);
+      FxAmp f[2] = {fx_load_amp<M>(c[0], E), fx_load_amp<M>(c[1], E)};
+      int64_t tr, ti;
+      fx_cdot<2>(&u.c[0], f, tr, ti);
+      out[j0] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      fx_cdot<2>(&u.c[2], f, tr, ti);
+      out[j0 | bit] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+    }
+  }
+}
+
+// 4x4 gate on bits q0 (matrix MSB) and q1
+template <typename IT>
+__global__ void __launch_bounds__(256) k_fxdense2(const double2* __restrict__ in, double2* out, IT nquads, int q0,
+                                                  int q1, const __grid_constant__ FxCoef16 u) {
+  constexpr int M = 57;
+  const int lo = q0 < q1 ? q0 : q1, hi = q0 < q1 ? q1 : q0;
+  const IT b0 = IT(1) << q0, b1 = IT(1) << q1;
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < nquads; t += nthr) {
+    const IT base = insert0(insert0(t, lo), hi);
+    const IT idx[4] = {base, base | b1, base | b0, base | b0 | b1};
+    double2 a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a[r] = in[idx[r]];
+    const int E = fx_group_exp<4>(a);
+    FxAmp f[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) f[r] = fx_load_amp<M>(a[r], E);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int64_t tr, ti;
+      fx_cdot<4>(&u.c[4 * r], f, tr, ti);
+      out[idx[r]] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+    }
+  }
+}
+
+// ----------------------------------------------------------- group pass ----
+constexpr int FXG_MAX_OPS = 64;
+constexpr int FXG_MAX_COEF = 640;
+struct FxGroupOp {
+  uint8_t type;    // OP_DENSE1 / OP_DENSE2 / OP_SIGN / OP_DIAG / OP_PHASE / OP_CUT
+  uint8_t a, b;    // dense: register-index bits (DENSE2: a = matrix MSB, a > b)
+  uint8_t k;       // DIAG: qubits
+  uint8_t gb[3];   // DIAG: global bits, matrix MSB first
+  uint8_t pad;
+  uint16_t coef;   // first coefficient
+  uint16_t ncoef;  // CUT: table size (index clamp)
+  uint16_t rmask;  // SIGN: registers whose group bits of the op are all set
+  uint16_t pad2;
+  uint64_t mout;   // SIGN: the op's global bits outside the group
+};
+struct FxGroupParams {
+  const double2* in;
+  double2* out;
+  const uint16_t* cuts;
+  int32_t n, nops;
+  uint8_t sbits[4];  // the group bits, ascending
+  int32_t pad;
+  int64_t off[16];   // global offset of register index r
+  FxGroupOp ops[FXG_MAX_OPS];
+  FxC coef[FXG_MAX_COEF];
+};
+
+template <int G, int J>
+QF_D void fxg_dense1(const FxC* cf, FxAmp (&v)[1 << G]) {
+#pragma unroll
+  for (int i = 0; i < (1 << (G - 1)); ++i) {
+    const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
+    const int i1 = i0 | (1 << J);
+    const FxAmp p[2] = {v[i0], v[i1]};
+    int64_t tr, ti;
+    fx_cdot<2>(cf, p, tr, ti);
+    v[i0] = fx_amp_from_t(tr, ti);
+    fx_cdot<2>(cf + 2, p, tr, ti);
+    v[i1] = fx_amp_from_t(tr, ti);
+  }
+}
+template <int G, int J0, int J1>
+QF_D void fxg_dense2(const FxC* cf, FxAmp (&v)[1 << G]) {
+  constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
+#pragma unroll
+  for (int i = 0; i < (1 << (G - 2)); ++i) {
+    int b = ((i >> LO) << (LO + 1)) | (i & ((1 << LO) - 1));
+    b = ((b >> HI) << (HI + 1)) | (b & ((1 << HI) - 1));
+    const int idx[4] = {b, b | (1 << J1), b | (1 << J0), b | (1 << J0) | (1 << J1)};
+    const FxAmp p[4] = {v[idx[0]], v[idx[1]], v[idx[2]], v[idx[3]]};
+    int64_t tr[4], ti[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) fx_cdot<4>(cf + 4 * r, p, tr[r], ti[r]);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) v[idx[r]] = fx_amp_from_t(tr[r], ti[r]);
+  }
+}
+template <int G>
+QF_D void fxg_dense1_dispatch(int j, const FxC* cf, FxAmp (&v)[1 << G]) {
+  if constexpr (G >= 1) {
+    switch (j) {
+      case 0: fxg_dense1<G, 0>(cf, v); break;
+      case 1: if constexpr (G > 1) fxg_dense1<G, 1>(cf, v); break;
+      case 2: if constexpr (G > 2) fxg_dense1<G, 2>(cf, v); break;
+      case 3: if constexpr (G > 3) fxg_dense1<G, 3>(cf, v); break;
+    }
+  }
+}
+template <int G>
+QF_D void fxg_dense2_dispatch(int a, int b, const FxC* cf, FxAmp (&v)[1 << G]) {
+  if constexpr (G >= 2) {
+    switch (a * 4 + b) {
+      case 4: fxg_dense2<G, 1, 0>(cf, v); break;
+      case 8: if constexpr (G > 2) fxg_dense2<G, 2, 0>(cf, v); break;
+      case 9: if constexpr (G > 2) fxg_dense2<G, 2, 1>(cf, v); break;
+      case 12: if constexpr (G > 3) fxg_dense2<G, 3, 0>(cf, v); break;
+      case 13: if constexpr (G > 3) fxg_dense2<G, 3, 1>(cf, v); break;
+      case 14: if constexpr (G > 3) fxg_dense2<G, 3, 2>(cf, v); break;
+    }
+  }
+}
+
+template <int G>
+QF_D void fxg_negate(uint32_t neg, FxAmp (&v)[1 << G]) {
+#pragma unroll
+  for (int r = 0; r < (1 << G); ++r)
+    if ((neg >> r) & 1u) v[r] = fx_neg(v[r]);
+}
+
+// one coefficient per amplitude: v[r] *= cf[index(r)]
+QF_D FxAmp fx_mul1(const FxC& c, const FxAmp& a) {
+  int64_t tr, ti;
+  fx_cdot<1>(&c, &a, tr, ti);
+  return fx_amp_from_t(tr, ti);
+}
+
+template <int G, typename IT>
+__global__ void __launch_bounds__(256) k_fxgroup(const __grid_constant__ FxGroupParams P) {
+  constexpr int R = 1 << G;
+  constexpr int M = G <= 2 ? 57 : 56;
+  const IT ngroups = IT(1) << (P.n - G);
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
+    IT xb = t;
+#pragma unroll
+    for (int j = 0; j < G; ++j) xb = insert0(xb, (int)P.sbits[j]);
+    double2 a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r] = P.in[xb | (IT)P.off[r]];
+    const int E = fx_group_exp<R>(a);
+    FxAmp v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = fx_load_amp<M>(a[r], E);
+    uint32_t neg = 0;  // CZ-like signs not yet applied
+    for (int o = 0; o < P.nops; ++o) {
+      const FxGroupOp& op = P.ops[o];
+      switch (op.type) {
+        case OP_SIGN:
+          if ((xb & (IT)op.mout) == (IT)op.mout) neg ^= op.rmask;
+          break;
+        case OP_DENSE1:
+          fxg_negate<G>(neg, v);
+          neg = 0;
+          fxg_dense1_dispatch<G>(op.a, &P.coef[op.coef], v);
+          break;
+        case OP_DENSE2:
+          fxg_negate<G>(neg, v);
+          neg = 0;
+          fxg_dense2_dispatch<G>(op.a, op.b, &P.coef[op.coef], v);
+          break;
+        case OP_DIAG:
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const IT x = xb | (IT)P.off[r];
+            int idx = 0;
+            for (int i = 0; i < op.k; ++i) idx = (idx << 1) | int((x >> op.gb[i]) & 1);
+            v[r] = fx_mul1(P.coef[op.coef + idx], v[r]);
+          }
+          break;
+        case OP_PHASE:
+#pragma unroll
+          for (int r = 0; r < R; ++r) v[r] = fx_mul1(P.coef[op.coef], v[r]);
+          break;
+        case OP_CUT:
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const IT x = xb | (IT)P.off[r];
+            const int c = min((int)P.cuts[x], (int)op.ncoef - 1);  // a foreign cut table cannot overrun
+            v[r] = fx_mul1(P.coef[op.coef + c], v[r]);
+          }
+          break;
+        default:
+          break;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) P.out[xb | (IT)P.off[r]] = fx_flip(fx_store_amp<M>(v[r], E), (neg >> r) & 1u);
+  }
+}
+
+// --------------------------------------------------------------- host ----
+namespace {
+
+constexpr double FX_UNIT_TOL = 1e-9;
+
+bool unit_modulus(cplx c) { return std::abs(std::abs(c) - 1.0) <= FX_UNIT_TOL; }
+
+// the fixed-point kernels take unitary gates only (their overflow bound
+// rests on the group norm being preserved)
+bool unitary(const std::vector<cplx>& m, int G) {
+  for (int i = 0; i < G; ++i)
+    for (int j = 0; j < G; ++j) {
+      cplx d(0, 0);
+      for (int k = 0; k < G; ++k) d += m[i * G + k] * std::conj(m[j * G + k]);
+      if (std::abs(d - (i == j ? cplx(1, 0) : cplx(0, 0))) > FX_UNIT_TOL) return false;
+    }
+  return true;
+}
+
+// kinds of op for the fixed-point planner
+enum FxKind { FXK_DENSE = 1, FXK_ELEM = 2, FXK_NATIVE = 3 };
+
+FxKind fx_kind(const HostOp& op) {
+  switch (op.type) {
+    case OP_DENSE1:
+    case OP_DENSE2:
+      return unitary(op.m, 1 << op.k) ? FXK_DENSE : FXK_NATIVE;
+    case OP_MONO:  // generalised permutations on <= 2 bits run as dense gates
+      if (op.k > 2) return FXK_NATIVE;
+      for (int r = 0; r < (1 << op.k); ++r)
+        if (!unit_modulus(op.diag[r])) return FXK_NATIVE;
+      return FXK_DENSE;
+    case OP_SIGN:
+      return FXK_ELEM;
+    case OP_DIAG:
+      if (op.k > 3) return FXK_NATIVE;
+      for (int r = 0; r < (1 << op.k); ++r)
+        if (!unit_modulus(op.diag[r])) return FXK_NATIVE;
+      return FXK_ELEM;
+    case OP_PHASE:
+      return unit_modulus(op.scalar) ? FXK_ELEM : FXK_NATIVE;
+    case OP_CUT:
+      for (const cplx& c : op.table)
+        if (!unit_modulus(c)) return FXK_NATIVE;
+      return FXK_ELEM;
+    default:
+      return FXK_NATIVE;  // dense gates on 3..5 qubits
+  }
+}
+
+int fx_coef_count(const HostOp& op) {
+  switch (op.type) {
+    case OP_DENSE1: return 4;
+    case OP_DENSE2: return 16;
+    case OP_MONO: return op.k == 1 ? 4 : 16;
+    case OP_DIAG: return 1 << op.k;
+    case OP_PHASE: return 1;
+    case OP_CUT: return (int)op.table.size();
+  }
+  return 0;
+}
+
+struct FxBlock {
+  std::vector<int> idx;
+  int order[4] = {0, 0, 0, 0};  // dense bits in order of first use
+  int G = 0;
+  bool native = false;  // one op run by the native FP64 kernels
+  int ncoef = 0;
+};
+
+constexpr int FX_G_MAX = 4;
+
+// Greedy passes: element-wise ops join the current pass; a dense op joins
+// while the pass's dense bits stay within gmax; ops the fixed-point kernels
+// do not take close the pass and run alone in native FP64.
+std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
+  if (fusion_k <= 0) fusion_k = FX_G_MAX;
+  if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
+  const int gmax = std::min(fusion_k, FX_G_MAX);
+  const bool fuse = fusion_k > 1;
+  std::vector<FxBlock> blocks;
+  FxBlock cur;
+  auto close = [&]() {
+    if (!cur.idx.empty()) blocks.push_back(cur);
+    cur = FxBlock();
+  };
+  for (int i = 0; i < (int)ops.size(); ++i) {
+    const HostOp& op = ops[i];
+    const FxKind kind = fx_kind(op);
+    const int need = fx_coef_count(op);
+    if (kind == FXK_NATIVE) {
+      close();
+      cur.idx.push_back(i);
+      cur.native = true;
+      close();
+      continue;
+    }
+    int add[2], nadd = 0;
+    if (kind == FXK_DENSE)
+      for (int j = 0; j < op.k; ++j)
+        if (std::find(cur.order, cur.order + cur.G, op.gb[j]) == cur.order + cur.G) add[nadd++] = op.gb[j];
+    const bool fits = cur.G + nadd <= gmax && (int)cur.idx.size() < FXG_MAX_OPS && cur.ncoef + need <= FXG_MAX_COEF;
+    if (!cur.idx.empty() && (!fuse || !fits)) close();
+    if (kind == FXK_DENSE) {
+      for (int j = 0; j < op.k; ++j)
+        if (std::find(cur.order, cur.order + cur.G, op.gb[j]) == cur.order + cur.G) cur.order[cur.G++] = op.gb[j];
+    }
+    cur.idx.push_back(i);
+    cur.ncoef += need;
+  }
+  close();
+  return blocks;
+}
+
+int grid_cap(int64_t items) {
+  const int64_t cap = (int64_t)device_sm_count() * 8;
+  int64_t g = (items + 255) / 256;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+std::vector<cplx> dense_matrix(const HostOp& op) {
+  const int D = 1 << op.k;
+  if (op.type != OP_MONO) return op.m;
+  std::vector<cplx> m((size_t)D * D, cplx(0, 0));
+  for (int r = 0; r < D; ++r) m[r * D + op.perm[r]] = op.diag[r];
+  return m;
+}
+
+int launch_fx_single(const void* in, void* out, int n, const HostOp& op, cudaStream_t stream) {
+  const double2* src = reinterpret_cast<const double2*>(in);
+  double2* dst = reinterpret_cast<double2*>(out);
+  const std::vector<cplx> m = dense_matrix(op);
+  if (op.k == 1) {
+    FxCoef4 u;
+    for (int i = 0; i < 4; ++i) u.c[i] = make_fxc(m[i].real(), m[i].imag());
+    const int64_t np = int64_t(1) << (n - 1);
+    const int grid = grid_cap((np + 1) / 2);
+    if (n <= 31)
+      k_fxdense1<uint32_t><<<grid, 256, 0, stream>>>(src, dst, (uint32_t)np, op.gb[0], u);
+    else
+      k_fxdense1<int64_t><<<grid, 256, 0, stream>>>(src, dst, np, op.gb[0], u);
+  } else {
+    FxCoef16 u;
+    for (int i = 0; i < 16; ++i) u.c[i] = make_fxc(m[i].real(), m[i].imag());
+    const int64_t nq = int64_t(1) << (n - 2);
+    if (n <= 31)
+      k_fxdense2<uint32_t><<<grid_cap(nq), 256, 0, stream>>>(src, dst, (uint32_t)nq, op.gb[0], op.gb[1], u);
+    else
+      k_fxdense2<int64_t><<<grid_cap(nq), 256, 0, stream>>>(src, dst, nq, op.gb[0], op.gb[1], u);
+  }
+  return check_cuda(cudaGetLastError());
+}
+
+// Fill the group parameters of block B (its dense bits become register bits:
+// the first-used bit is the top register bit).
+int fx_group_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, FxGroupParams& P) {
+  const int G = B.G;
+  if (n - G < 0 || (int)B.idx.size() > FXG_MAX_OPS) return QF_ERR_NOT_SUPPORTED;
+  std::memset(&P, 0, sizeof(FxGroupParams));
+  P.n = n;
+  int reg_of[64];
+  std::fill(reg_of, reg_of + 64, -1);
+  int rbits[4] = {0, 0, 0, 0};
+  uint64_t gmask = 0;
+  for (int k = 0; k < G; ++k) {
+    rbits[G - 1 - k] = B.order[k];
+    reg_of[B.order[k]] = G - 1 - k;
+    gmask |= uint64_t(1) << B.order[k];
+  }
+  int sb[4];
+  for (int j = 0; j < G; ++j) sb[j] = rbits[j];
+  std::sort(sb, sb + G);
+  for (int j = 0; j < G; ++j) P.sbits[j] = (uint8_t)sb[j];
+  for (int r = 0; r < (1 << G); ++r) {
+    int64_t o = 0;
+    for (int j = 0; j < G; ++j)
+      if ((r >> j) & 1) o |= int64_t(1) << rbits[j];
+    P.off[r] = o;
+  }
+  int nc = 0, no = 0;
+  auto put = [&](cplx v) { P.coef[nc++] = make_fxc(v.real(), v.imag()); };
+  for (int i : B.idx) {
+    const HostOp& op = ops[i];
+    FxGroupOp& g = P.ops[no++];
+    const int need = fx_coef_count(op);
+    if (nc + need > FXG_MAX_COEF) return QF_ERR_NOT_SUPPORTED;
+    g.coef = (uint16_t)nc;
+    const bool dense = op.type == OP_DENSE1 || op.type == OP_DENSE2 || op.type == OP_MONO;
+    if (dense) {
+      const std::vector<cplx> m = dense_matrix(op);
+      if (op.k == 1) {
+        g.type = OP_DENSE1;
+        g.a = (uint8_t)reg_of[op.gb[0]];
+        for (int e = 0; e < 4; ++e) put(m[e]);
+      } else {
+        g.type = OP_DENSE2;
+        const int ja = reg_of[op.gb[0]], jb = reg_of[op.gb[1]];
+        const bool swap = ja < jb;
+        g.a = (uint8_t)(swap ? jb : ja);
+        g.b = (uint8_t)(swap ? ja : jb);
+        auto sw = [](int x) { return ((x & 1) << 1) | (x >> 1); };  // exchange the two index bits
+        for (int r = 0; r < 4; ++r)
+          for (int c = 0; c < 4; ++c) put(swap ? m[sw(r) * 4 + sw(c)] : m[r * 4 + c]);
+      }
+      continue;
+    }
+    g.type = op.type;
+    switch (op.type) {
+      case OP_SIGN: {
+        uint64_t msk = 0;
+        int jm = 0;
+        for (int j = 0; j < op.k; ++j) {
+          msk |= uint64_t(1) << op.gb[j];
+          if (reg_of[op.gb[j]] >= 0) jm |= 1 << reg_of[op.gb[j]];
+        }
+        g.mout = msk & ~gmask;
+        uint32_t rm = 0;
+        for (int r = 0; r < (1 << G); ++r)
+          if ((r & jm) == jm) rm |= 1u << r;
+        g.rmask = (uint16_t)rm;
+        break;
+      }
+      case OP_DIAG:
+        g.k = (uint8_t)op.k;
+        for (int j = 0; j < op.k; ++j) g.gb[j] = (uint8_t)op.gb[j];
+        for (int e = 0; e < (1 << op.k); ++e) put(op.diag[e]);
+        break;
+      case OP_PHASE:
+        put(op.scalar);
+        break;
+      case OP_CUT:
+        g.ncoef = (uint16_t)op.table.size();
+        for (const cplx& c : op.table) put(c);
+        P.cuts = op.cuts;
+        break;
+      default:
+        return QF_ERR_NOT_SUPPORTED;
+    }
+  }
+  P.nops = no;
+  return QF_OK;
+}
+
+using FxGroupKernel = void (*)(FxGroupParams);
+const FxGroupKernel kFxGroup32[5] = {k_fxgroup<0, uint32_t>, k_fxgroup<1, uint32_t>, k_fxgroup<2, uint32_t>,
+                                     k_fxgroup<3, uint32_t>, k_fxgroup<4, uint32_t>};
+const FxGroupKernel kFxGroup64[5] = {k_fxgroup<0, int64_t>, k_fxgroup<1, int64_t>, k_fxgroup<2, int64_t>,
+                                     k_fxgroup<3, int64_t>, k_fxgroup<4, int64_t>};
+
+int fx_group_launch(const FxGroupParams& P, int G, cudaStream_t stream) {
+  const int64_t ngroups = int64_t(1) << (P.n - G);
+  (P.n <= 31 ? kFxGroup32 : kFxGroup64)[G]<<<grid_cap(ngroups), 256, 0, stream>>>(P);
+  return check_cuda(cudaGetLastError());
+}
+
+// kernel used by a block: 0 element-wise group pass, 1 direct sweep,
+// 3 group pass, 5 native FP64 op
+int fx_block_kernel(const std::vector<HostOp>& ops, const FxBlock& B) {
+  if (B.native) return 5;
+  if (B.G == 0) return 0;
+  if (B.idx.size() == 1) return 1;
+  return 3;
+}
+
+}  // namespace
+
+int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int fusion_k, cudaStream_t stream,
+               int* passes_out) {
+  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k);
+  int passes = 0;
+  const void* src = in;
+  if (blocks.empty()) {
+    if (in != out) {
+      const size_t bytes = (size_t(1) << n) * 16;
+      int rc = check_cuda(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, stream));
+      if (rc) return rc;
+      passes = 1;
+    }
+    if (passes_out) *passes_out = passes;
+    return QF_OK;
+  }
+  static thread_local FxGroupParams gp;  // ~17 KiB: kept off the stack
+  for (FxBlock& B : blocks) {
+    int rc;
+    switch (fx_block_kernel(ops, B)) {
+      case 5: {
+        std::vector<HostOp> one(1, ops[B.idx[0]]);
+        int p = 0;
+        rc = run_ops(src, out, n, C128, one, 1, stream, &p);
+        break;
+      }
+      case 1: {
+        LaunchTimer timer(ops[B.idx[0]].k == 1 ? QF_KERNEL_FX_DENSE1 : QF_KERNEL_FX_DENSE2, stream);
+        rc = launch_fx_single(src, out, n, ops[B.idx[0]], stream);
+        break;
+      }
+      default: {
+        rc = fx_group_prepare(n, ops, B, gp);
+        if (rc) return rc;
+        gp.in = reinterpret_cast<const double2*>(src);
+        gp.out = reinterpret_cast<double2*>(out);
+        LaunchTimer timer(B.G == 0 ? QF_KERNEL_FX_ELEMENTWISE : QF_KERNEL_FX_GROUP, stream);
+        rc = fx_group_launch(gp, B.G, stream);
+        break;
+      }
+    }
+    if (rc) return rc;
+    ++passes;
+    src = out;
+  }
+  if (passes_out) *passes_out = passes;
+  return QF_OK;
+}
+
+int fx_plan_stats(int n, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks, int* nblocks) {
+  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k);
+  *nblocks = (int)blocks.size();
+  for (int b = 0; b < (int)blocks.size() && b < max_blocks; ++b) {
+    const FxBlock& B = blocks[b];
+    int32_t* st = stats + 8 * b;
+    std::memset(st, 0, 8 * sizeof(int32_t));
+    st[0] = (int32_t)B.idx.size();
+    for (int i : B.idx) {
+      const HostOp& op = ops[i];
+      const bool dense = op.type == OP_DENSE1 || op.type == OP_DENSE2 || op.type == OP_MONO;
+      if (dense && op.k == 1) st[1]++;
+      else if (dense && op.k == 2) {
+        st[2]++;
+        if (op.gb[0] < 5 || op.gb[1] < 5) st[3]++;
+      } else if (op.type == OP_DIAG || op.type == OP_SIGN || op.type == OP_PHASE || op.type == OP_CUT) st[4]++;
+      else st[5]++;
+    }
+    uint64_t hm = 0;
+    for (int j = 0; j < B.G; ++j) hm |= uint64_t(1) << B.order[j];
+    st[6] = __builtin_popcountll(hm & ~uint64_t(31));
+    const int kk = fx_block_kernel(ops, B);
+    st[7] = kk == 0 ? 0 : kk == 1 ? 1 : kk == 3 ? 3 : 5;
+  }
+  return QF_OK;
+}
+
+}  // namespace qf

@@ -20,9 +20,12 @@
 //     needs clearing between calls, but two calls whose kernels overlap on
 //     the GPU (different streams, or different host threads) race on the
 //     array and may return wrong values.  Serialise such calls.
-//   - The first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture begins.
+//   - Every call that is not being captured into a CUDA graph looks up the
+//     array's device address (cudaGetSymbolAddress) with the calling device
+//     current, so the address stays right after a device reset reloads the
+//     library's module; a call made while its stream is capturing reuses
+//     the address its device's last uncaptured call found.  Make one call
+//     on each device before any stream capture begins.
 #include <mutex>
 
 #include "engine.cuh"
@@ -32,6 +35,11 @@ namespace qf {
 
 static __device__ __align__(256) double g_noalloc_partials[2 * QF_NOALLOC_MAX_PARTIALS];
 
+// Every reduction launch fits the array: the header's promise (any n up to
+// QF_MAX_QUBITS) holds as long as this does.
+static_assert(REDUCE_MAX_BLOCKS <= QF_NOALLOC_MAX_PARTIALS,
+              "reduction block count exceeds the no-allocation partial-sum array");
+
 namespace {
 
 // Device address of g_noalloc_partials per device.  In host code the symbol
@@ -40,13 +48,16 @@ namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_addr[64] = {nullptr};
 
-int noalloc_scratch(double** out) {
+int noalloc_scratch(cudaStream_t stream, double** out) {
   int dev = 0;
   int rc = check_cuda(cudaGetDevice(&dev));
   if (rc) return rc;
   if (dev < 0 || dev >= 64) return QF_ERR_NOT_SUPPORTED;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  rc = check_cuda(cudaStreamIsCapturing(stream, &cap));
+  if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
+  if (cap == cudaStreamCaptureStatusNone || g_noalloc_addr[dev] == nullptr) {
     void* p = nullptr;
     rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_partials));
     if (rc) return rc;
@@ -62,14 +73,15 @@ int noalloc_scratch(double** out) {
 extern "C" int qf_expectation_cuts_noalloc(const void* psi, int n, int layout, const uint16_t* cuts,
                                            double* out, void* stream) {
   using namespace qf;
-  if (layout != C64 && layout != C128 && layout != FF) return QF_ERR_LAYOUT;
+  if (layout != C64 && layout != C128 && layout != FF && layout != FX) return QF_ERR_LAYOUT;
+  if (layout == FX) layout = C128;  // the same complex128 bytes
   if (n > QF_MAX_QUBITS) return QF_ERR_TOO_LARGE;
   if (n < 1 || psi == nullptr || cuts == nullptr || out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   if ((reinterpret_cast<uintptr_t>(psi) & 15u) != 0) return QF_ERR_ALIGNMENT;
   if (reduce_blocks(int64_t(1) << n) > QF_NOALLOC_MAX_PARTIALS) return QF_ERR_TOO_LARGE;
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   double* partials = nullptr;
-  int rc = noalloc_scratch(&partials);
+  int rc = noalloc_scratch(s, &partials);
   if (rc) return rc;
-  return reduce_diag(psi, n, layout, 1, cuts, nullptr, out, partials,
-                     reinterpret_cast<cudaStream_t>(stream));
+  return reduce_diag(psi, n, layout, 1, cuts, nullptr, out, partials, s);
 }

@@ -25,7 +25,7 @@
 
 namespace qf {
 
-enum Layout : int { C64 = 0, C128 = 1, FF = 2 };
+enum Layout : int { C64 = 0, C128 = 1, FF = 2, FX = 3 };  // FX: C128 storage, fixed-point gates
 
 // ---------------------------------------------------------------- types ----
 template <int L> struct Types;

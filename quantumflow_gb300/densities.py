@@ -18,7 +18,7 @@ import torch
 
 from . import _native as nat
 from .qubits import Qubits, outer_product, qubits_count_tuple, QubitVector
-from .states import Buffer, State, _DTYPES, _as_complex_tensor, _device, compute_layout
+from .states import Buffer, State, _DTYPES, _as_complex_tensor, _device, compute_layout, gate_layout
 
 __all__ = ["Density", "mixed_density", "random_density", "join_densities"]
 
@@ -136,7 +136,7 @@ def evolve_gates(rho: Density, gates) -> Density:
     op_axes = np.asarray(axes, dtype=np.int32)
     op_mats = np.ascontiguousarray(np.concatenate(mats))
     passes = (nat.ctypes.c_int * 1)()
-    nat.call("qf_run_circuit", nat.ptr(src.data), nat.ptr(out.data), src.n, src.layout, len(ks),
+    nat.call("qf_run_circuit", nat.ptr(src.data), nat.ptr(out.data), src.n, gate_layout(src), len(ks),
              op_k.ctypes.data_as(nat._ip), op_axes.ctypes.data_as(nat._ip), op_mats.ctypes.data_as(nat._dp),
              0, passes, nat.stream_handle(src.device))
     return Density(out, rho.qubits, rho._memory)
@@ -154,7 +154,7 @@ def evolve_superop(rho: Density, superop: np.ndarray, qubits: Qubits) -> Density
     m = np.ascontiguousarray(np.asarray(superop, dtype=np.complex128).reshape(4 ** k, 4 ** k))
     src = rho.buffer.compute()
     out = src.empty_like()
-    nat.call("qf_apply_gate", nat.ptr(src.data), nat.ptr(out.data), src.n, src.layout, 2 * k,
+    nat.call("qf_apply_gate", nat.ptr(src.data), nat.ptr(out.data), src.n, gate_layout(src), 2 * k,
              nat.int_array(axes), m.view(np.float64).reshape(-1).ctypes.data_as(nat._dp),
              nat.stream_handle(src.device))
     return Density(out, rho.qubits, rho._memory)

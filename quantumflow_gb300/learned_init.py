@@ -9,7 +9,10 @@ optimised from the network's angles and from the linear ramp, recording the
 initial ratio <C>/max C and the steps and wall time to reach a target ratio.
 
 Usage:  python -m quantumflow_gb300.learned_init [--count 20000] [--out PATH]
-The default weights live in ``quantumflow_gb300/data/angle_gnn_p6.npz``.
+        python -m quantumflow_gb300.learned_init --evaluate [--eval-count 1000] [--report PATH]
+The default weights live in ``quantumflow_gb300/data/angle_gnn_p6.npz``;
+``--evaluate`` evaluates them without training, and the 1,000-graph report
+of that run is ``quantumflow_gb300/data/angle_gnn_p6_eval.json``.
 """
 import argparse
 import json
@@ -177,8 +180,14 @@ def main():
     ap.add_argument("--eval-count", type=int, default=1000)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--evaluate", action="store_true", help="evaluate the stored weights, no training")
     args = ap.parse_args()
-    net, stats = train(count=args.count, label_steps=args.label_steps, epochs=args.epochs, out=args.out)
+    if args.evaluate:
+        net = AngleGNN.load(args.out)
+        stats = {"weights": os.path.basename(args.out), "eval_count": args.eval_count, "eval_n": [12, 22],
+                 "eval_seed": 777, "target": 0.9, "steps": 300, "lr": 0.05, "dtype": "complex64"}
+    else:
+        net, stats = train(count=args.count, label_steps=args.label_steps, epochs=args.epochs, out=args.out)
     ev = evaluate(net, count=args.eval_count)
     stats["evaluation"] = ev
     print(json.dumps(stats, indent=1))

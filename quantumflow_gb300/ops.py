@@ -10,10 +10,11 @@ from abc import ABC
 from typing import Any, Dict
 
 import numpy as np
+import torch
 
 from . import _native as nat
 from .qubits import Qubits, QubitVector, asarray
-from .states import State
+from .states import State, gate_layout
 
 __all__ = ["Operation", "Gate"]
 
@@ -119,8 +120,15 @@ class Gate(Operation):
         src = ket.buffer.compute()
         out = src.empty_like()
         k = len(indices)
+        if k > nat.MAX_GATE_QUBITS:
+            # wide dense gate: the matrix goes to the device (it does not fit
+            # the kernel parameters of qf_apply_gate)
+            dmat = torch.from_numpy(np.ascontiguousarray(self.asoperator(), dtype=np.complex128)).to(src.device)
+            nat.call("qf_apply_dense_gate", nat.ptr(src.data), nat.ptr(out.data), src.n, gate_layout(src), k,
+                     nat.int_array(indices), nat.ptr(dmat), nat.stream_handle(src.device))
+            return State(out, ket.qubits, ket._memory)
         mat = np.ascontiguousarray(self.matrix_doubles())
-        nat.call("qf_apply_gate", nat.ptr(src.data), nat.ptr(out.data), src.n, src.layout, k,
+        nat.call("qf_apply_gate", nat.ptr(src.data), nat.ptr(out.data), src.n, gate_layout(src), k,
                  nat.int_array(indices), mat.ctypes.data_as(nat._dp), nat.stream_handle(src.device))
         return State(out, ket.qubits, ket._memory)
 

@@ -23,7 +23,7 @@ import torch
 from . import _native as nat
 from . import config
 from .circuits import Circuit
-from .states import Buffer, State, _device, _reduce, compute_layout
+from .states import Buffer, State, _device, _reduce
 from .stdgates import H, RX, RZ, ZZ
 
 __all__ = ["qubo_circuit", "graph_cuts", "Graph", "gnp_random_graph", "random_regular_graph",
@@ -130,6 +130,15 @@ def random_regular_graph(d: int, n: int, seed=None, max_tries: int = 10000) -> G
             g.add_edge(int(a), int(b))
         return g
     raise RuntimeError("random_regular_graph: too many rejections")
+
+
+def compute_layout(dtype: str) -> int:
+    """Element layout of the QAOA kernels' state buffers: complex64, or for
+    complex128 float-float pairs, or native FP64 when that is configured
+    (config.C128_ARITHMETIC == "fp64")."""
+    if dtype == "complex64":
+        return nat.LAYOUT_C64
+    return nat.LAYOUT_C128 if config.C128_ARITHMETIC == "fp64" else nat.LAYOUT_FF
 
 
 def _graph_arrays(graph):

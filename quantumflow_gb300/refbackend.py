@@ -20,6 +20,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from . import config as _config
 from .config import version as _version
 
 BACKEND = "gb300"
@@ -204,10 +205,17 @@ def tensormul(tensor0, tensor1, indices):
     shape = tuple(state.shape)
     N = len(shape)
     state = state.reshape(-1).contiguous()
+    out = torch.empty_like(state)
+    layout = nat.LAYOUT_FX if _config.C128_ARITHMETIC == "fx" else nat.LAYOUT_C128
+    if K > nat.MAX_GATE_QUBITS:
+        # wide gates: the matrix stays on (or goes to) the device
+        dmat = astensor(tensor0).reshape(-1).contiguous()
+        nat.call("qf_apply_dense_gate", nat.ptr(state), nat.ptr(out), N, layout, K, nat.int_array(list(indices)),
+                 nat.ptr(dmat), nat.stream_handle(state.device))
+        return out.reshape(shape)
     gate = tensor0.detach().to("cpu", torch.complex128) if _is_t(tensor0) else \
         torch.from_numpy(np.asarray(tensor0, dtype=np.complex128))
     mat = np.ascontiguousarray(gate.reshape(2 ** K, 2 ** K).numpy()).view(np.float64).reshape(-1)
-    out = torch.empty_like(state)
-    nat.call("qf_apply_gate", nat.ptr(state), nat.ptr(out), N, nat.LAYOUT_C128, K,
+    nat.call("qf_apply_gate", nat.ptr(state), nat.ptr(out), N, layout, K,
              nat.int_array(list(indices)), mat.ctypes.data_as(nat._dp), nat.stream_handle(state.device))
     return out.reshape(shape)

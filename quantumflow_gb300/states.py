@@ -6,9 +6,11 @@ device buffer of 2^N amplitudes; amplitudes are never copied to the host
 unless the caller asks for them (``asarray``, ``print_state``).
 
 Element layouts (include/qf_gb300.h): complex64 states use QF_LAYOUT_C64.
-complex128 states are computed either in float-float (QF_LAYOUT_FF, the
-default) or native FP64 (QF_LAYOUT_C128), see config.C128_ARITHMETIC.  An FF
-buffer is converted back to complex128 only when ``State.tensor`` is read.
+complex128 states are held as complex128 (QF_LAYOUT_C128) and their gates
+run in 64-bit integer fixed point (the engine's QF_LAYOUT_FX argument, the
+default) or native FP64, or they are held as float-float pairs
+(QF_LAYOUT_FF), see config.C128_ARITHMETIC.  An FF buffer is converted back
+to complex128 only when ``State.tensor`` is read.
 """
 import math
 from collections import defaultdict
@@ -36,9 +38,19 @@ def _device():
 
 
 def compute_layout(dtype: str) -> int:
+    """Element layout of the buffers gates are applied to."""
     if dtype == "complex64":
         return nat.LAYOUT_C64
     return nat.LAYOUT_FF if config.C128_ARITHMETIC == "ff" else nat.LAYOUT_C128
+
+
+def gate_layout(buf: "Buffer") -> int:
+    """The layout argument of the gate-engine calls (qf_apply_gate,
+    qf_run_circuit) for ``buf``: complex128 buffers run the fixed-point
+    arithmetic (QF_LAYOUT_FX, same bytes) unless native FP64 is configured."""
+    if buf.layout == nat.LAYOUT_C128 and config.C128_ARITHMETIC == "fx":
+        return nat.LAYOUT_FX
+    return buf.layout
 
 
 class Buffer:
@@ -58,7 +70,7 @@ class Buffer:
         device = device or _device()
         if layout == nat.LAYOUT_C64:
             data = torch.empty(2 ** n, dtype=torch.complex64, device=device)
-        elif layout == nat.LAYOUT_C128:
+        elif layout in (nat.LAYOUT_C128, nat.LAYOUT_FX):
             data = torch.empty(2 ** n, dtype=torch.complex128, device=device)
         elif layout == nat.LAYOUT_FF:
             data = torch.empty((2 ** n, 4), dtype=torch.float32, device=device)

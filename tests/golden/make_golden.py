@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Runs ONLY in the build container, where the read-only QuantumFlow reference
-checkout exists (default ``/root/reference``; override with ``QF_REFERENCE``).
-The GPU machine never runs this script: it only reads the ``.npz`` files it wrote.
+Runs only where a read-only QuantumFlow reference checkout exists; its path
+is given by the ``QF_REFERENCE`` environment variable (the script stops when
+it is unset).  The GPU tests never run this script: they only read the
+``.npz`` files it wrote.
 
 What it does:
 
@@ -19,7 +20,7 @@ What it does:
   named below);
 * runs the reference on seeded inputs and stores inputs and outputs.
 
-Usage:  PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+Usage:  QF_REFERENCE=<checkout> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [name ...]
 """
 import ast
 import importlib.abc
@@ -30,7 +31,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("QF_REFERENCE", "/root/reference")
+REF = os.environ.get("QF_REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 STUBBED = ("pyquil", "cvxpy", "PIL")
 
@@ -78,6 +79,8 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
 
 def import_reference():
     """Import the reference package (numpy backend) with the stubs above."""
+    if not REF or not os.path.isdir(os.path.join(REF, "quantumflow")):
+        sys.exit("set QF_REFERENCE to a QuantumFlow checkout (the directory holding quantumflow/)")
     os.environ.setdefault("QUANTUMFLOW_BACKEND", "numpy")
     sys.dont_write_bytecode = True
     sys.meta_path.insert(0, _StubFinder())
@@ -444,6 +447,66 @@ def channel_fixtures(qf, rng):
     return out
 
 
+# ------------------------------------ random-layer family at bench sizes ----
+def layer_family_fixtures(qf, rng):
+    """The benchmark's circuit family (Haar U(2) on every qubit, then CZ on a
+    seeded random perfect matching, per layer) run by the reference's
+    Circuit.run (quantumflow/circuits.py:87-99, one numpy einsum per gate):
+    N=16 and N=20 with all 100 layers, N=24 with 2 layers.  The gates are
+    stored; of the output, N=16 keeps the full state and every size keeps
+    4096 amplitudes at seeded indices (first and last included), the
+    probabilities of the top 8 axes (marginal over the rest) and the norm."""
+    out = {}
+    for N, layers in ((16, 100), (20, 100), (24, 2)):
+        ops = random_layer_circuit(N, layers, rng)
+        circ = qf.Circuit()
+        us, pairs = [], []
+        for kind, qs, u in ops:
+            if kind == 1:
+                circ += qf.Gate(u, qubits=qs)
+                us.append(u)
+            else:
+                circ += qf.CZ(*qs)
+                pairs.append(qs)
+        ket = circ.run(qf.zero_state(N))
+        psi = np.asarray(ket.tensor).reshape(-1)
+        idx = np.unique(np.concatenate([[0, 2 ** N - 1], rng.choice(2 ** N, size=4094, replace=False)]))
+        out[f"lf{N}_layers"] = np.array(layers)
+        out[f"lf{N}_u"] = np.array(us)                      # [layers * N, 2, 2], layer-major
+        out[f"lf{N}_pairs"] = np.array(pairs, dtype=np.int64).reshape(layers, N // 2, 2)
+        out[f"lf{N}_idx"] = idx.astype(np.int64)
+        out[f"lf{N}_amps"] = psi[idx]
+        out[f"lf{N}_top8"] = (np.abs(psi) ** 2).reshape(256, -1).sum(axis=1)
+        out[f"lf{N}_norm"] = np.array(float(np.vdot(psi, psi).real))
+        if N <= 16:
+            out[f"lf{N}_state"] = psi
+        print(f"  layer family N={N}: {len(ops)} gates", flush=True)
+    return out
+
+
+# ---------------------------------------------------- wide tensormul ----
+def tensormul_wide_fixtures(qf, rng):
+    """quantumflow/backend/numpybk.py:159-214 tensormul with K = 4..7 gate
+    qubits (random complex gate tensors, not unitary) on states of N <= 10
+    qubits, on scattered axes."""
+    bk = qf.backend
+    out = {}
+    cases = [(6, 4), (8, 5), (9, 6), (10, 7), (7, 7)]
+    for c, (N, K) in enumerate(cases):
+        idx = rng.choice(N, size=K, replace=False)
+        state = rng.normal(size=2 ** N) + 1j * rng.normal(size=2 ** N)
+        gate = rng.normal(size=(2 ** K, 2 ** K)) + 1j * rng.normal(size=(2 ** K, 2 ** K))
+        res = bk.tensormul(bk.astensorproduct(gate.reshape([2] * (2 * K))),
+                           bk.astensorproduct(state), list(int(i) for i in idx))
+        out[f"tw{c}_N"] = np.array(N)
+        out[f"tw{c}_idx"] = np.array(idx)
+        out[f"tw{c}_gate"] = gate
+        out[f"tw{c}_state"] = state
+        out[f"tw{c}_out"] = np.asarray(res).reshape(-1)
+    out["tw_count"] = np.array(len(cases))
+    return out
+
+
 def main():
     qf = import_reference()
     rng = np.random.default_rng(20181203)
@@ -455,6 +518,8 @@ def main():
         "qaoa.npz": lambda: qaoa_fixtures(qf, rng),
         "programs.npz": lambda: program_fixtures(qf, np.random.default_rng(20181204)),
         "channels.npz": lambda: channel_fixtures(qf, np.random.default_rng(20181205)),
+        "layers.npz": lambda: layer_family_fixtures(qf, np.random.default_rng(20181206)),
+        "tensormul_wide.npz": lambda: tensormul_wide_fixtures(qf, np.random.default_rng(20181207)),
     }
     only = set(sys.argv[1:])  # e.g. `programs` to rewrite programs.npz alone
     for fname, arrays in files.items():

@@ -17,6 +17,14 @@ def _circuit_from_fixture(c, N):
     return circ
 
 
+@pytest.fixture(params=["fx", "ff", "fp64"])
+def arith(request, monkeypatch):
+    """complex128 arithmetic: fixed point (default), float-float, native FP64."""
+    import quantumflow_gb300 as qf
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", request.param)
+    return request.param
+
+
 @pytest.fixture(params=[0, 1, 2, 4], ids=["default", "smem_tiles", "warp_rb2", "warp_rb4"])
 def tile_kernel(request):
     from quantumflow_gb300 import _native as nat
@@ -27,7 +35,7 @@ def tile_kernel(request):
 
 @pytest.mark.parametrize("dtype,tol", [("complex128", 1e-12), ("complex64", 1e-5)])
 @pytest.mark.parametrize("fusion_k", [1, 2, 4, 6, 8])
-def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k, tile_kernel):
+def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k, tile_kernel, arith):
     import quantumflow_gb300 as qf
     c = golden["circuits"]
     for N in (4, 6, 9, 12):
@@ -43,11 +51,11 @@ def test_reference_random_layer_circuits(golden, dtype, tol, fusion_k, tile_kern
         assert err < tol * 2, (N, err)
 
 
-@pytest.mark.parametrize("arith", ["ff", "fp64"])
-def test_kat_circuits(golden, arith, monkeypatch):
+@pytest.mark.parametrize("c128", ["fx", "ff", "fp64"])
+def test_kat_circuits(golden, c128, monkeypatch):
     import quantumflow_gb300 as qf
     from math import pi
-    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", arith)
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", c128)
     kat = golden["kat"]
     circ = qf.Circuit()
     circ += qf.RY(pi / 2, 0)
@@ -85,7 +93,7 @@ def test_gops_circuit(golden):
 
 @pytest.mark.parametrize("N", [13, 16, 22])
 @pytest.mark.parametrize("dtype", ["complex128", "complex64"])
-def test_fused_equals_unfused_and_oracle(N, dtype, tile_kernel):
+def test_fused_equals_unfused_and_oracle(N, dtype, tile_kernel, arith):
     """Mixed gate classes through every fused-kernel instruction: 1q gates on
     lane, register and warp bits, 2q dense gates, permutations, diagonals."""
     import quantumflow_gb300 as qf
@@ -142,7 +150,7 @@ def test_large_round_trip(N):
 @pytest.mark.parametrize("N", [9, 12, 17])
 @pytest.mark.parametrize("dtype", ["complex128", "complex64"])
 @pytest.mark.parametrize("fusion_k", [0, 3])
-def test_gate_merging_equals_unmerged_and_oracle(N, dtype, fusion_k, tile_kernel):
+def test_gate_merging_equals_unmerged_and_oracle(N, dtype, fusion_k, tile_kernel, arith):
     """Host gate merging (blocks of <= 2 qubits) and the warp kernel's lane
     exchanges for 2-qubit gates on lane bits: the merged run equals the
     unmerged run and the oracle."""
@@ -209,7 +217,7 @@ def test_gate_merging_random_layers_n20():
 
 
 @pytest.mark.parametrize("merge", [0, 1])
-def test_shape_passes_random_programs(merge):
+def test_shape_passes_random_programs(merge, monkeypatch):
     """Float-float fused passes split into straight-line shape kernels (one
     or two dense gates with CZ signs around them): random programs of Haar
     1- and 2-qubit gates and CZs, mostly on the low (lane) bits where the
@@ -219,6 +227,7 @@ def test_shape_passes_random_programs(merge):
     import ctypes
     import quantumflow_gb300 as qf
     from quantumflow_gb300 import _native as nat
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", "ff")
     N = 12
     rng = np.random.default_rng(77 + merge)
     low = list(range(N - 5, N))  # axes of bits 0..4
@@ -263,16 +272,20 @@ def test_shape_passes_random_programs(merge):
     assert seen_shapes >= 10
 
 
-def test_index_paths_above_2_31_amplitudes():
+@pytest.mark.parametrize("c128", ["ff", "fx"])
+def test_index_paths_above_2_31_amplitudes(c128, monkeypatch):
     """States of more than 2^31 amplitudes take the 64-bit-index forms of the
-    4x4 sweep and the shape kernels: N=32 float-float (64 GB per state,
-    128 GB at the peak), two merged random layers and their inverse must
-    return |0...0> -- norm and single-qubit marginals by device reductions,
-    no host copy of the state."""
+    4x4 sweep and the shape kernels (float-float) or of the fixed-point
+    group and sweep kernels: N=32 complex128 (64 GB per state, 128 GB at the
+    peak), two merged random layers and their inverse must return |0...0> --
+    norm and single-qubit marginals by device reductions, no host copy of
+    the state."""
     import ctypes
     import quantumflow_gb300 as qf
     from quantumflow_gb300 import _native as nat
     from quantumflow_gb300.states import _reduce
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", c128)
+    layout = nat.LAYOUT_FF if c128 == "ff" else nat.LAYOUT_FX
     N = 32
     free, _ = torch.cuda.mem_get_info()
     if free < 150 * 2 ** 30:
@@ -290,10 +303,11 @@ def test_index_paths_above_2_31_amplitudes():
     op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
     stats = np.zeros(8 * 512, np.int32)
     nb = ctypes.c_int()
-    assert nat.lib.qf_plan_circuit(N, nat.LAYOUT_FF, nops, op_k.ctypes.data, op_axes.ctypes.data,
+    assert nat.lib.qf_plan_circuit(N, layout, nops, op_k.ctypes.data, op_axes.ctypes.data,
                                    op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
     kinds = set(stats[:8 * nb.value].reshape(-1, 8)[:, 7])
-    assert {1, 4} <= kinds  # lone sweeps and shape passes both run
+    # lone sweeps and shape passes (float-float) / group passes (fixed point)
+    assert ({1, 4} if c128 == "ff" else {3}) <= kinds
     ket = circ.run(qf.zero_state(N))
     assert abs(ket.norm() - 1) < 1e-11
     back = circ.H.run(ket)
@@ -338,6 +352,7 @@ def test_autotune_fusion_and_shape_width(tmp_path, monkeypatch):
         perm = rng.permutation(N)
         for a in range(0, N - 1, 2):
             circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", "ff")  # shape widths are a float-float setting
     best = autotune.tune_fusion(circ, N, candidates=(0, 2), modes=(0,), reps=1)
     assert {t["shape_bits"] for t in best["trials"]} == {2, 3, 4}
     cached = autotune.fusion_config("complex128", N)

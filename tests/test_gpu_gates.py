@@ -10,10 +10,10 @@ from oracle import qf_oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-# tolerances: complex128 (FP64 and float-float arithmetic) 1e-12 max amplitude
-# error, complex64 1e-5 (the parity bar of this backend)
-TOL = {0: 1e-5, 1: 1e-12, 2: 1e-12}
-LAYOUTS = [0, 1, 2]
+# tolerances: complex128 (FP64, float-float and fixed-point arithmetic) 1e-12
+# max amplitude error, complex64 1e-5 (the parity bar of this backend)
+TOL = {0: 1e-5, 1: 1e-12, 2: 1e-12, 3: 1e-12}
+LAYOUTS = [0, 1, 2, 3]
 
 
 def _run(state_np, mat, axes, layout):
@@ -121,7 +121,16 @@ def test_errors_raise():
     ket = qf.zero_state(3)
     with pytest.raises(ValueError):
         qf.H(7).run(ket)  # unknown qubit label (reference ops.py:164 list.index)
-    with pytest.raises(NativeError):
-        qf.Gate(np.eye(64), qubits=range(6)).run(qf.zero_state(8))  # k > 5
     from quantumflow_gb300 import _native as nat
+    fake = nat._vp(0x10000)
+    m = np.eye(64, dtype=np.complex128).view(np.float64).reshape(-1)
+    # host-matrix entry point: k > 5 is for qf_apply_dense_gate
+    assert nat.lib.qf_apply_gate(fake, fake, 8, 1, 6, nat.int_array(range(6)), m.ctypes.data_as(nat._dp),
+                                 None) == 6
+    # device-matrix entry point: k above QF_MAX_DENSE_QUBITS, misaligned matrix
+    assert nat.lib.qf_apply_dense_gate(fake, fake, 14, 1, 13, nat.int_array(range(13)), fake, None) == 6
+    assert nat.lib.qf_apply_dense_gate(fake, fake, 8, 1, 6, nat.int_array(range(6)), nat._vp(0x10008),
+                                       None) == 4
+    with pytest.raises(NativeError):  # unknown layout
+        nat.call("qf_apply_dense_gate", fake, fake, 8, 9, 6, nat.int_array(range(6)), fake, None)
     assert nat.device_error() == 0

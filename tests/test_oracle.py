@@ -143,3 +143,25 @@ def test_oracle_matches_reference_channels(golden):
                                c["damping_superop"], atol=1e-15)
     ket = c["ket"]
     np.testing.assert_allclose(np.outer(ket, ket.conj()), c["ket_density"], atol=1e-15)
+
+
+def test_layer_family_n16_matches_reference():
+    """The benchmark's circuit family at N=16, all 100 layers (2400 gates),
+    against the reference's Circuit.run output."""
+    from tests.conftest import load_golden
+    lf = load_golden("layers.npz")
+    ops = orc.layer_family_ops(lf["lf16_u"], lf["lf16_pairs"])
+    assert len(ops) == 2400
+    st = orc.run_ops(orc.zero_state(16), ops).reshape(-1)
+    np.testing.assert_allclose(st, lf["lf16_state"], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(st[lf["lf16_idx"]], lf["lf16_amps"], rtol=0, atol=1e-13)
+
+
+def test_tensormul_wide_matches_reference():
+    """tensormul with K = 4..7 gate qubits (numpybk.py:159-214) against the
+    reference's outputs."""
+    from tests.conftest import load_golden
+    g = load_golden("tensormul_wide.npz")
+    for c in range(int(g["tw_count"])):
+        out = orc.tensormul(g[f"tw{c}_gate"], g[f"tw{c}_state"], [int(i) for i in g[f"tw{c}_idx"]])
+        np.testing.assert_allclose(out.reshape(-1), g[f"tw{c}_out"], rtol=0, atol=1e-11)

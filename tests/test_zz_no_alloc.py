@@ -28,15 +28,17 @@ def _noalloc_result(nat, buf, cuts):
     return float(out.item())
 
 
-@pytest.mark.parametrize("layout", [0, 1, 2])
+@pytest.mark.parametrize("layout", [0, 1, 2, 3])
 def test_noalloc_matches_workspace_entry_point(layout):
     import quantumflow_gb300 as qf
     from quantumflow_gb300 import _native as nat
     tol = 1e-5 if layout == 0 else 1e-12  # relative, as in the other parity tests
     rng = np.random.default_rng(11)
-    # two calls in a row with different sizes: the second uses fewer blocks,
-    # so stale partial sums from the first call sit in the shared array
-    for n, p in ((18, 2), (12, 3), (12, 3)):
+    # calls in a row with different sizes: n=23 fills the array up to the
+    # block cap of the reduction (8 blocks per SM), the later ones use fewer
+    # blocks, so stale partial sums from the earlier calls sit in the
+    # shared array
+    for n, p in ((23, 1), (18, 2), (12, 3), (12, 3)):
         g = qf.qaoa.random_regular_graph(3, n, seed=n)
         prob = qf.QAOAMaxCut(g, p, dtype="complex64" if layout == 0 else "complex128")
         beta, gamma = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)
