@@ -326,6 +326,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2018)
     ap.add_argument("--tile-mode", type=int, default=0, help="qf_set_tile_kernel mode (0 = default)")
     ap.add_argument("--shape-bits", type=int, default=None, help="qf_set_shape_bits (default: library)")
+    ap.add_argument("--fx-occupancy", type=int, default=None, help="qf_set_fx_occupancy (default: library)")
     ap.add_argument("--merge", type=int, default=1, choices=[0, 1, 2],
                     help="qf_set_gate_merging: 1 merge (default), 2 merge + pass packing, 0 off")
     ap.add_argument("--no-qaoa", action="store_true", help="skip the QAOA time-to-ratio measurement")
@@ -363,6 +364,8 @@ def main():
     if args.shape_bits is not None:
         nat.call("qf_set_shape_bits", args.shape_bits)
     nat.call("qf_set_gate_merging", args.merge)
+    if args.fx_occupancy is not None:
+        nat.call("qf_set_fx_occupancy", args.fx_occupancy)
 
     N, S = args.n, (16 if args.dtype == "complex128" else 8)
     sweep_bytes = 2 * S * 2 ** N
@@ -422,10 +425,12 @@ def main():
         torch.cuda.synchronize()
         nat.timing_enable(False)
         sk = nat.timing_collect()
-        sms, scount = sk["dense1"]
+        kind = "fx_dense1" if sk["fx_dense1"][1] else "dense1"
+        sms, scount = sk[kind]
         if scount:
             sweep_ach = sweep_bytes / (sms / scount * 1e-3) / 1e9
-            sweep = {"kernel": "k_dense1 (one 2x2 gate per pass, all 28 qubits)", "achieved": sweep_ach,
+            kname = "k_fxdense1" if kind == "fx_dense1" else "k_dense1"
+            sweep = {"kernel": f"{kname} (one 2x2 gate per pass, all {N} qubits)", "achieved": sweep_ach,
                      "peak": None, "unit": "GB/s", "frac": None, "launches_timed": scount}
 
     peak, peak_kind = measured_peaks()

@@ -95,7 +95,8 @@ size_t qf_reduce_workspace_bytes(int n);
 #define QF_KERNEL_FX_DENSE2 9      /* fixed-point 4x4 sweep                       */
 #define QF_KERNEL_FX_GROUP 10      /* fixed-point fused pass on a register group  */
 #define QF_KERNEL_FX_ELEMENTWISE 11 /* fixed-point pass of element-wise ops only  */
-#define QF_KERNEL_CLASSES 12
+#define QF_KERNEL_FX_SHAPE 12      /* fixed-point straight-line pass (1-2 gates)  */
+#define QF_KERNEL_CLASSES 13
 int qf_timing_enable(int on);
 /* Fused-pass kernel selection (diagnostics and tests; no reference
  * counterpart), process-wide: 0 = default (float-float group passes --
@@ -125,8 +126,9 @@ int qf_set_gate_merging(int on);
  * in stats[8*b ..]: ops, dense 1-qubit, dense 2-qubit, of those with a lane
  * bit (< 5), element-wise, other, high bits (>= 5), kernel (0 element-wise,
  * 1 direct single-gate sweep, 2 fused warp-tile or shared-memory pass,
- * 3 float-float group pass, 4 float-float shape pass).  *nblocks gets the
- * pass count; at most max_blocks rows are written. */
+ * 3 group pass, 4 shape pass, 5 one gate in native FP64 inside a
+ * QF_LAYOUT_FX circuit).  *nblocks gets the pass count; at most max_blocks
+ * rows are written. */
 int qf_plan_circuit(int n, int layout, int nops, const int* op_k, const int* op_axes, const double* op_mats,
                     int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
 int qf_timing_collect(double* ms, int64_t* launches, int nkinds);
@@ -160,6 +162,16 @@ int qf_apply_gate(const void* psi_in, void* psi_out, int n, int layout, int k, c
  * float-float state is converted to complex128 in psi_out and back). */
 int qf_apply_dense_gate(const void* psi_in, void* psi_out, int n, int layout, int k, const int* axes,
                         const double* matrix, void* stream);
+/* Dense complex64 gates on 5 or 6 qubits (n >= k + 7) run on the tensor
+ * cores (tcgen05 MMAs, TF32 operands split into hi + lo parts, FP32
+ * accumulation) unless this is 0 (then the CUDA-core kernel); default 1.
+ * Process-wide; diagnostics and tests, no reference counterpart. */
+int qf_set_dense_tensor_cores(int on);
+/* Fixed-point (QF_LAYOUT_FX) straight-line passes on 3 and 4 gate bits:
+ * compile them for at least min_blocks resident CTAs of 128 threads per SM
+ * (1..4; the register cap trades per-thread registers for warps), states of
+ * at most 2^31 amplitudes.  Process-wide tuning, no reference counterpart. */
+int qf_set_fx_occupancy(int min_blocks);
 
 /* Apply nops gates in order with gate fusion.  Replaces the per-gate loop of
  * quantumflow/circuits.py:87-99 Circuit.run.  Gate i acts on op_k[i] axes

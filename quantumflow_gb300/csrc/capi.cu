@@ -16,6 +16,8 @@ extern int g_warp_rb_override;
 extern int g_merge_gates;
 extern int g_group_kernel;
 extern int g_shape_max_bits;
+extern int g_dense_tensor_cores;
+extern int g_fx_min_blocks;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int apply_dense_gate(const void* in, void* out, int n, int layout, int k, const int* bits, const double* mat,
                      cudaStream_t stream);
@@ -118,6 +120,18 @@ int qf_set_tile_kernel(int mode) {
   g_adjoint_smem_only = mode == 1;
   g_warp_rb_override = mode >= 2 && mode <= 4 ? mode : 0;
   g_group_kernel = mode == 5 ? 0 : 1;
+  return QF_OK;
+}
+
+int qf_set_fx_occupancy(int min_blocks) {
+  if (min_blocks < 1 || min_blocks > 4) return QF_ERR_INVALID_ARGUMENT;
+  g_fx_min_blocks = min_blocks;
+  return QF_OK;
+}
+
+int qf_set_dense_tensor_cores(int on) {
+  if (on < 0 || on > 1) return QF_ERR_INVALID_ARGUMENT;
+  g_dense_tensor_cores = on;
   return QF_OK;
 }
 

@@ -16,7 +16,9 @@
 // with shuffles.  Every group is owned by one CTA and fully staged before
 // its outputs are written, so the gate may be applied in place.
 // complex64 states compute in FP32, complex128 in FP64; float-float states
-// are converted to complex128 in place around the FP64 kernel.
+// are converted to complex128 in place around the FP64 kernel.  Dense
+// complex64 gates on 5 or 6 qubits take the tensor cores instead
+// (tcdense.cu) unless qf_set_dense_tensor_cores(0).
 #include <algorithm>
 #include <atomic>
 #include <cstring>
@@ -26,6 +28,8 @@
 namespace qf {
 
 int convert(const void* src, int sl, void* dst, int dl, int n, cudaStream_t stream);
+int tc_dense_gate(const void* in, void* out, int n, int k, const int* bits, const double* mat, cudaStream_t stream);
+int g_dense_tensor_cores = 1;  // qf_set_dense_tensor_cores
 
 constexpr int DENSEK_MAX = QF_MAX_DENSE_QUBITS;
 
@@ -188,6 +192,10 @@ int apply_dense_gate(const void* in, void* out, int n, int layout, int k, const 
   std::sort(P.sbits, P.sbits + k);
   switch (layout) {
     case C64:
+      if (g_dense_tensor_cores) {
+        const int rc = tc_dense_gate(in, out, n, k, bits, mat, stream);
+        if (rc != QF_ERR_NOT_SUPPORTED) return rc;
+      }
       return densek_dispatch<float2>(P, stream);
     case C128:
     case FX:

@@ -227,6 +227,12 @@ struct ShapeParams {
 // planner splits fused float-float passes at the points where the next
 // dense gate would leave the table.
 int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd);
+// The table shape of ops[dense[0..nd)] whatever the width limit: returns its
+// index (or -1), the bits in order of first use (order[0] is register bit
+// G-1), G, which 4x4 slots have their matrix MSB on the lower register bit
+// (swap[]), and the slot codes.
+int shape_lookup(const std::vector<HostOp>& ops, const int* dense, int nd, int* order, int& G, bool* swap,
+                 int* s0, int* s1);
 // Fill P for the pass ops[idx] (dense gates and sign ops only) and launch
 // it; QF_ERR_NOT_SUPPORTED when it is not a table shape.
 int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::vector<int>& idx,

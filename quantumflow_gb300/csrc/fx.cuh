@@ -12,19 +12,24 @@
 //    keep theirs down to the same absolute quantum;
 //  * gates: a coefficient c (|c| <= 1, unitary gates only) is the integer
 //    C = round(c * 2^58).  Both are held as two int32 pieces,
-//    A = Ah * 2^28 + Al and C = Ch * 2^28 + Cl, and a row of a gate is
+//    A = Ah * 2^28 + Al and C = Ch * 2^28 + Cl, and a real dot product is
 //        sum_k A_k C_k = 2^56 sum Ah Ch + 2^28 sum (Ah Cl + Al Ch) + sum Al Cl
 //    accumulated exactly in two int64 registers (three IMAD.WIDE per real
 //    product); the last term (< 2^56 per product, a quarter of the result's
-//    quantum) is dropped and the result is rounded to the quantum of A;
+//    quantum) is dropped and the result is rounded to the quantum of A.  A
+//    complex row sum_j u_j a_j takes three real dot products (Gauss's
+//    three-multiplication complex product): P1 = sum ur ar, P2 = sum ui ai,
+//    P3 = sum (ur + ui)(ar + ai); re = P1 - P2, im = P3 - P1 - P2;
 //  * store: each part is rounded once to the nearest FP64 value.
 //
 // Unitary gates preserve the 2-norm of a thread's amplitude group, so no
-// intermediate exceeds 2^(M + 0.5 + G/2) < 2^59 and nothing overflows.  The
-// error of one pass is below a quarter of the quantum per product plus the
-// final FP64 rounding: at least 55 significant bits relative to the group's
-// largest part, against the 53 of FP64 arithmetic.  Gates that are not
-// unitary run in native FP64 (the host planner routes them).
+// part exceeds 2^(M + 0.5 + G/2) and no sum ar + ai exceeds 2^(M + 1 + G/2)
+// <= 2^58.5 (M = 56 for G <= 2, 55 for G <= 4): the pieces fit int32 and the
+// accumulators int64.  The error of one pass is below a quarter of the
+// quantum per product plus the final FP64 rounding: at least 55 significant
+// bits relative to the group's largest part, against the 53 of FP64
+// arithmetic.  Gates that are not unitary run in native FP64 (the host
+// planner routes them).  Parts must stay below 2^1000 in magnitude.
 #pragma once
 #include <cstdint>
 #include <cmath>
@@ -37,23 +42,23 @@ constexpr int FX_F = 58;  // coefficient fraction bits
 constexpr int FX_L = 28;  // piece split position
 constexpr uint32_t FX_LMASK = (1u << FX_L) - 1u;
 
-// One complex coefficient: re, im and -im, each as (hi, lo) pieces with
+// One complex coefficient: re, im and re + im, each as (hi, lo) pieces with
 // C = hi * 2^28 + lo, 0 <= lo < 2^28.
 struct FxC {
-  int32_t rh, rl, ih, il, nh, nl;
+  int32_t rh, rl, ih, il, sh, sl;
 };
 
-// Host: pieces of round(v * 2^58), |v| <= 1 + 1e-9.
-inline void fx_pieces(double v, int32_t& h, int32_t& l) {
-  const long long c = std::llround(std::ldexp(v, FX_F));
+// Host: pieces of C = round(v * 2^58), |v| <= 1.5.
+inline void fx_pieces(long long c, int32_t& h, int32_t& l) {
   h = static_cast<int32_t>(c >> FX_L);  // arithmetic shift: floor
   l = static_cast<int32_t>(c & static_cast<long long>(FX_LMASK));
 }
 inline FxC make_fxc(double re, double im) {
   FxC c;
-  fx_pieces(re, c.rh, c.rl);
-  fx_pieces(im, c.ih, c.il);
-  fx_pieces(-im, c.nh, c.nl);
+  const long long cr = std::llround(std::ldexp(re, FX_F)), ci = std::llround(std::ldexp(im, FX_F));
+  fx_pieces(cr, c.rh, c.rl);
+  fx_pieces(ci, c.ih, c.il);
+  fx_pieces(cr + ci, c.sh, c.sl);  // exactly the sum of the rounded parts
   return c;
 }
 
@@ -134,14 +139,16 @@ constexpr int FX_EMIN = 64;
 
 // The part v as A = ah * 2^28 + al relative to the group exponent E >= e(v):
 // A = v * 2^(1022 + M - E), truncated toward zero; |al| < 2^28.
+// E comes from fx_group_exp, which raises groups below FX_EMIN out of range
+// (every part of such a group becomes 0).
 template <int M>
 QF_HD void fx_in(double v, int E, int32_t& ah, int32_t& al) {
   const uint32_t hi = fx_hiword(v), lo = fx_loword(v);
   const int e = static_cast<int>((hi >> 20) & 0x7ffu);
   // right shift of the 64-bit mantissa with its hidden bit at bit 63
-  uint32_t r = static_cast<uint32_t>(E - e) + static_cast<uint32_t>(64 - M);
-  if (e == 0 || E < FX_EMIN) r = 127u;
-  const uint32_t mh = fx_shl64hi(lo, hi, 11) | 0x80000000u;
+  // (zeros and subnormals carry no hidden bit and become 0)
+  const uint32_t r = static_cast<uint32_t>(E - e) + static_cast<uint32_t>(64 - M);
+  const uint32_t mh = fx_shl64hi(lo, hi, 11) | (e != 0 ? 0x80000000u : 0u);
   const uint32_t ml = lo << 11;
   const uint32_t h = fx_shr(mh, r - 4u);        // A >> 28 (r >= 64 - M >= 7)
   const uint32_t x = fx_shr64lo(ml, mh, r);     // low word of A for r < 32
@@ -183,8 +190,7 @@ QF_HD double fx_out(int64_t T, int E) {
   const uint64_t q = ((static_cast<uint64_t>(qh) << 32) | ql) + inc;
   qh = static_cast<uint32_t>(q >> 32);
   ql = static_cast<uint32_t>(q);
-  int eb = E + 62 - M - lz;  // biased exponent; the hidden bit of q adds one
-  if (eb > 2046) eb = 2046;
+  const int eb = E + 62 - M - lz;  // biased exponent; the hidden bit of q adds one
   const uint32_t bits_hi = (qh + (static_cast<uint32_t>(eb - 1) << 20)) | (s & 0x80000000u);
   return fx_double(bits_hi, ql);
 }
@@ -219,22 +225,24 @@ struct FxAmp {
   int32_t rh, rl, ih, il;
 };
 
-// out = sum_j u[j] a[j] (J terms) as T values (units of A / 4).
+// out = sum_j u[j] a[j] (J terms) as T values (units of A / 4): three real
+// dot products (P1 = sum ur ar, P2 = sum ui ai, P3 = sum (ur+ui)(ar+ai)).
 template <int J>
 QF_HD void fx_cdot(const FxC* u, const FxAmp* a, int64_t& tre, int64_t& tim) {
-  FxAcc re, im;
-  re.zero();
-  im.zero();
+  FxAcc p1, p2, p3;
+  p1.zero();
+  p2.zero();
+  p3.zero();
 #pragma unroll
   for (int j = 0; j < J; ++j) {
     const FxC c = u[j];
-    re.add(a[j].rh, a[j].rl, c.rh, c.rl);
-    re.add(a[j].ih, a[j].il, c.nh, c.nl);
-    im.add(a[j].ih, a[j].il, c.rh, c.rl);
-    im.add(a[j].rh, a[j].rl, c.ih, c.il);
+    p1.add(a[j].rh, a[j].rl, c.rh, c.rl);
+    p2.add(a[j].ih, a[j].il, c.ih, c.il);
+    p3.add(a[j].rh + a[j].ih, a[j].rl + a[j].il, c.sh, c.sl);
   }
-  tre = re.total();
-  tim = im.total();
+  const int64_t t1 = p1.total(), t2 = p2.total(), t3 = p3.total();
+  tre = t1 - t2;
+  tim = t3 - t1 - t2;
 }
 
 QF_HD FxAmp fx_amp_from_t(int64_t tre, int64_t tim) {

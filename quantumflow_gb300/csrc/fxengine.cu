@@ -9,10 +9,11 @@
 // Kernels:
 //   k_fxdense1  one 2x2 gate on any bit (a thread holds two amplitude pairs)
 //   k_fxdense2  one 4x4 gate on any two bits (a thread holds one quad)
-//   k_fxgroup<G> an op list on a group of 2^G amplitudes per thread (the
-//               pass's dense gate bits, G <= 4), with sign (CZ-like),
-//               diagonal, phase and cut-table ops; G = 0 is a pass of
-//               element-wise ops only
+//   k_fxgroup<G> an op program on a group of 2^G amplitudes per thread (the
+//               pass's dense gate bits, G <= 4): 2x2 and 4x4 gates at one
+//               canonical register place with register-bit exchanges
+//               between them, sign (CZ-like), diagonal and phase ops; G = 0
+//               is a pass of element-wise ops only
 // Each kernel converts the amplitudes it holds to fixed point once, applies
 // its gates, and rounds to FP64 once.
 #include <algorithm>
@@ -32,7 +33,8 @@ QF_D int fx_group_exp(const double2 (&v)[R]) {
     m = max(m, fx_hiword(v[r].x) & 0x7fffffffu);
     m = max(m, fx_hiword(v[r].y) & 0x7fffffffu);
   }
-  return static_cast<int>(m >> 20);
+  const int E = static_cast<int>(m >> 20);
+  return E < FX_EMIN ? 4095 : E;  // a group of parts below 2^-959 becomes all zero
 }
 
 template <int M>
@@ -129,34 +131,211 @@ __global__ void __launch_bounds__(256) k_fxdense2(const double2* __restrict__ in
 }
 
 // ----------------------------------------------------------- group pass ----
-constexpr int FXG_MAX_OPS = 64;
+// A thread holds the 2^G amplitudes of the pass's gate bits; register-index
+// bit j holds one of those global bits, as the host tracks it.  Gates run in
+// one canonical place -- a 2x2 gate on register bit G-1, a 4x4 gate with
+// its matrix MSB on bit G-1 and LSB on bit G-2 -- and the host inserts
+// register-bit exchanges (FXI_SWAP) to bring each gate's bits there, so the
+// kernel holds one body per gate kind instead of one per bit combination.
+constexpr int FXG_MAX_OPS = 96;
 constexpr int FXG_MAX_COEF = 640;
+enum FxInstr : uint8_t {
+  FXI_SWAP = 1,    // exchange register-index bits a < b
+  FXI_DENSE1 = 2,  // 2x2 on register bit G-1
+  FXI_DENSE2 = 3,  // 4x4, MSB on bit G-1, LSB on bit G-2
+  FXI_SIGN = 4,    // negate registers rmask when the bits mout of xb are set
+  FXI_DIAG = 5,    // diagonal on k <= 3 bits (register bit rb[i], or global bit gb[i] of xb)
+  FXI_PHASE = 6,   // global scalar
+};
 struct FxGroupOp {
-  uint8_t type;    // OP_DENSE1 / OP_DENSE2 / OP_SIGN / OP_DIAG / OP_PHASE / OP_CUT
-  uint8_t a, b;    // dense: register-index bits (DENSE2: a = matrix MSB, a > b)
+  uint8_t type;
+  uint8_t a, b;    // SWAP: register bits, a < b
   uint8_t k;       // DIAG: qubits
-  uint8_t gb[3];   // DIAG: global bits, matrix MSB first
-  uint8_t pad;
+  int8_t rb[3];    // DIAG: register bit of the op's bit i (MSB first), -1 outside the group
+  uint8_t gb[3];   // DIAG: global bit of the op's bit i
   uint16_t coef;   // first coefficient
-  uint16_t ncoef;  // CUT: table size (index clamp)
   uint16_t rmask;  // SIGN: registers whose group bits of the op are all set
-  uint16_t pad2;
   uint64_t mout;   // SIGN: the op's global bits outside the group
 };
 struct FxGroupParams {
   const double2* in;
   double2* out;
-  const uint16_t* cuts;
   int32_t n, nops;
-  uint8_t sbits[4];  // the group bits, ascending
+  uint8_t sbits[4];     // the group bits, ascending
   int32_t pad;
-  int64_t off[16];   // global offset of register index r
+  int64_t off_in[16];   // global offset of register index r at load
+  int64_t off_out[16];  // ... at store (after the pass's exchanges)
   FxGroupOp ops[FXG_MAX_OPS];
   FxC coef[FXG_MAX_COEF];
 };
 
-template <int G, int J>
+// 2x2 on register bit G-1
+template <int G>
 QF_D void fxg_dense1(const FxC* cf, FxAmp (&v)[1 << G]) {
+  constexpr int H = 1 << (G - 1);
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const FxAmp p[2] = {v[i], v[i + H]};
+    int64_t tr, ti;
+    fx_cdot<2>(cf, p, tr, ti);
+    v[i] = fx_amp_from_t(tr, ti);
+    fx_cdot<2>(cf + 2, p, tr, ti);
+    v[i + H] = fx_amp_from_t(tr, ti);
+  }
+}
+// 4x4 with its MSB on register bit G-1 and LSB on bit G-2
+template <int G>
+QF_D void fxg_dense2(const FxC* cf, FxAmp (&v)[1 << G]) {
+  constexpr int Q = 1 << (G - 2);
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const FxAmp p[4] = {v[i], v[i + Q], v[i + 2 * Q], v[i + 3 * Q]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int64_t tr, ti;
+      fx_cdot<4>(cf + 4 * r, p, tr, ti);
+      v[i + r * Q] = fx_amp_from_t(tr, ti);
+    }
+  }
+}
+// exchange register-index bits A < B (register moves only)
+template <int G, int A, int B>
+QF_D void fxg_swap(FxAmp (&v)[1 << G]) {
+#pragma unroll
+  for (int r = 0; r < (1 << G); ++r)
+    if (((r >> A) & 1) && !((r >> B) & 1)) {
+      const int s = r ^ (1 << A) ^ (1 << B);
+      const FxAmp t = v[r];
+      v[r] = v[s];
+      v[s] = t;
+    }
+}
+template <int G>
+QF_D void fxg_swap_dispatch(int a, int b, FxAmp (&v)[1 << G]) {
+  if constexpr (G >= 2) {
+    switch (a * 4 + b) {
+      case 1: fxg_swap<G, 0, 1>(v); break;
+      case 2: if constexpr (G > 2) fxg_swap<G, 0, 2>(v); break;
+      case 6: if constexpr (G > 2) fxg_swap<G, 1, 2>(v); break;
+      case 3: if constexpr (G > 3) fxg_swap<G, 0, 3>(v); break;
+      case 7: if constexpr (G > 3) fxg_swap<G, 1, 3>(v); break;
+      case 11: if constexpr (G > 3) fxg_swap<G, 2, 3>(v); break;
+    }
+  }
+}
+
+template <int G>
+QF_D void fxg_negate(uint32_t neg, FxAmp (&v)[1 << G]) {
+#pragma unroll
+  for (int r = 0; r < (1 << G); ++r)
+    if ((neg >> r) & 1u) v[r] = fx_neg(v[r]);
+}
+
+// one coefficient per amplitude: v *= c
+QF_D FxAmp fx_mul1(const FxC& c, const FxAmp& a) {
+  int64_t tr, ti;
+  fx_cdot<1>(&c, &a, tr, ti);
+  return fx_amp_from_t(tr, ti);
+}
+
+constexpr int FXG_THREADS = 128;
+
+template <int G, typename IT>
+__global__ void __launch_bounds__(FXG_THREADS) k_fxgroup(const __grid_constant__ FxGroupParams P) {
+  constexpr int R = 1 << G;
+  constexpr int M = G <= 2 ? 57 : 56;
+  const IT ngroups = IT(1) << (P.n - G);
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
+    IT xb = t;
+#pragma unroll
+    for (int j = 0; j < G; ++j) xb = insert0(xb, (int)P.sbits[j]);
+    double2 a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[r] = P.in[xb | (IT)P.off_in[r]];
+    const int E = fx_group_exp<R>(a);
+    FxAmp v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = fx_load_amp<M>(a[r], E);
+    uint32_t neg = 0;  // CZ-like signs not yet applied (register mask)
+    for (int o = 0; o < P.nops; ++o) {
+      const FxGroupOp& op = P.ops[o];
+      switch (op.type) {
+        case FXI_SIGN:
+          if ((xb & (IT)op.mout) == (IT)op.mout) neg ^= op.rmask;
+          break;
+        case FXI_SWAP:
+          fxg_negate<G>(neg, v);
+          neg = 0;
+          fxg_swap_dispatch<G>(op.a, op.b, v);
+          break;
+        case FXI_DENSE1:
+          if constexpr (G >= 1) {
+            fxg_negate<G>(neg, v);
+            neg = 0;
+            fxg_dense1<G>(&P.coef[op.coef], v);
+          }
+          break;
+        case FXI_DENSE2:
+          if constexpr (G >= 2) {
+            fxg_negate<G>(neg, v);
+            neg = 0;
+            fxg_dense2<G>(&P.coef[op.coef], v);
+          }
+          break;
+        case FXI_DIAG:
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            int idx = 0;
+            for (int i = 0; i < op.k; ++i) {
+              const int bit = op.rb[i] >= 0 ? (r >> op.rb[i]) & 1 : int((xb >> op.gb[i]) & 1);
+              idx = (idx << 1) | bit;
+            }
+            v[r] = fx_mul1(P.coef[op.coef + idx], v[r]);
+          }
+          break;
+        case FXI_PHASE:
+#pragma unroll
+          for (int r = 0; r < R; ++r) v[r] = fx_mul1(P.coef[op.coef], v[r]);
+          break;
+        default:
+          break;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      P.out[xb | (IT)P.off_out[r]] = fx_flip(fx_store_amp<M>(v[r], E), (neg >> r) & 1u);
+  }
+}
+
+// ---------------------------------------------------------- shape passes ----
+// Straight-line passes for the common programs: one or two dense gates
+// (slots) at fixed register bits -- the shape table shared with the
+// float-float engine (group.cu): slot code 10 + j is a 2x2 gate on register
+// bit j, 100 + 10 j0 + j1 a 4x4 gate with its matrix MSB on bit j0 and LSB on
+// j1 -- with CZ-like signs before, between and after the slots.  The
+// coefficients sit at fixed parameter offsets (slot s at coef[16 s]), so the
+// products read them as constant operands.  Signs before the first slot and
+// after the last flip FP64 sign bits (exact); only signs between the slots
+// negate fixed-point registers.
+constexpr int FXS_THREADS = 128;
+struct FxShapeParams {
+  const double2* in;
+  double2* out;
+  int32_t n, shape;
+  int32_t sign_end[3];  // signs [sign_end[b-1], sign_end[b]) act before slot b (b = 2: after the last)
+  int32_t pad;
+  uint8_t sbits[4];     // the group bits, ascending
+  int32_t pad2;
+  int64_t off[16];      // global offset of register index r
+  uint16_t rmask[SHAPE_MAX_SIGNS];
+  uint64_t mout[SHAPE_MAX_SIGNS];
+  FxC coef[32];         // slot s at coef[16 s]
+};
+
+// 2x2 on register bit J / 4x4 with MSB on register bit J0 and LSB on J1
+template <int G, int J>
+QF_D void fxs_dense1(const FxC* cf, FxAmp (&v)[1 << G]) {
 #pragma unroll
   for (int i = 0; i < (1 << (G - 1)); ++i) {
     const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
@@ -170,7 +349,7 @@ QF_D void fxg_dense1(const FxC* cf, FxAmp (&v)[1 << G]) {
   }
 }
 template <int G, int J0, int J1>
-QF_D void fxg_dense2(const FxC* cf, FxAmp (&v)[1 << G]) {
+QF_D void fxs_dense2(const FxC* cf, FxAmp (&v)[1 << G]) {
   constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
 #pragma unroll
   for (int i = 0; i < (1 << (G - 2)); ++i) {
@@ -185,49 +364,19 @@ QF_D void fxg_dense2(const FxC* cf, FxAmp (&v)[1 << G]) {
     for (int r = 0; r < 4; ++r) v[idx[r]] = fx_amp_from_t(tr[r], ti[r]);
   }
 }
-template <int G>
-QF_D void fxg_dense1_dispatch(int j, const FxC* cf, FxAmp (&v)[1 << G]) {
-  if constexpr (G >= 1) {
-    switch (j) {
-      case 0: fxg_dense1<G, 0>(cf, v); break;
-      case 1: if constexpr (G > 1) fxg_dense1<G, 1>(cf, v); break;
-      case 2: if constexpr (G > 2) fxg_dense1<G, 2>(cf, v); break;
-      case 3: if constexpr (G > 3) fxg_dense1<G, 3>(cf, v); break;
-    }
-  }
-}
-template <int G>
-QF_D void fxg_dense2_dispatch(int a, int b, const FxC* cf, FxAmp (&v)[1 << G]) {
-  if constexpr (G >= 2) {
-    switch (a * 4 + b) {
-      case 4: fxg_dense2<G, 1, 0>(cf, v); break;
-      case 8: if constexpr (G > 2) fxg_dense2<G, 2, 0>(cf, v); break;
-      case 9: if constexpr (G > 2) fxg_dense2<G, 2, 1>(cf, v); break;
-      case 12: if constexpr (G > 3) fxg_dense2<G, 3, 0>(cf, v); break;
-      case 13: if constexpr (G > 3) fxg_dense2<G, 3, 1>(cf, v); break;
-      case 14: if constexpr (G > 3) fxg_dense2<G, 3, 2>(cf, v); break;
-    }
+template <int G, int S>
+QF_D void fxs_slot(const FxC* cf, FxAmp (&v)[1 << G]) {
+  if constexpr (S >= 100) {
+    fxs_dense2<G, (S / 10) % 10, S % 10>(cf, v);
+  } else if constexpr (S >= 10) {
+    fxs_dense1<G, S - 10>(cf, v);
   }
 }
 
-template <int G>
-QF_D void fxg_negate(uint32_t neg, FxAmp (&v)[1 << G]) {
-#pragma unroll
-  for (int r = 0; r < (1 << G); ++r)
-    if ((neg >> r) & 1u) v[r] = fx_neg(v[r]);
-}
-
-// one coefficient per amplitude: v[r] *= cf[index(r)]
-QF_D FxAmp fx_mul1(const FxC& c, const FxAmp& a) {
-  int64_t tr, ti;
-  fx_cdot<1>(&c, &a, tr, ti);
-  return fx_amp_from_t(tr, ti);
-}
-
-template <int G, typename IT>
-__global__ void __launch_bounds__(256) k_fxgroup(const __grid_constant__ FxGroupParams P) {
+template <int G, int S0, int S1, typename IT, int MINB = 1>
+__global__ void __launch_bounds__(FXS_THREADS, MINB) k_fxshape(const __grid_constant__ FxShapeParams P) {
   constexpr int R = 1 << G;
-  constexpr int M = G <= 2 ? 57 : 56;
+  constexpr int M = G <= 2 ? 56 : 55;
   const IT ngroups = IT(1) << (P.n - G);
   const IT nthr = (IT)gridDim.x * blockDim.x;
   for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
@@ -237,56 +386,58 @@ __global__ void __launch_bounds__(256) k_fxgroup(const __grid_constant__ FxGroup
     double2 a[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) a[r] = P.in[xb | (IT)P.off[r]];
+    auto signs = [&](int s0, int s1) {
+      uint32_t m = 0;
+      for (int s = s0; s < s1; ++s)
+        if ((xb & (IT)P.mout[s]) == (IT)P.mout[s]) m ^= P.rmask[s];
+      return m;
+    };
+    if (P.sign_end[0] > 0) {
+      const uint32_t m = signs(0, P.sign_end[0]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) a[r] = fx_flip(a[r], (m >> r) & 1u);
+    }
     const int E = fx_group_exp<R>(a);
     FxAmp v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = fx_load_amp<M>(a[r], E);
-    uint32_t neg = 0;  // CZ-like signs not yet applied
-    for (int o = 0; o < P.nops; ++o) {
-      const FxGroupOp& op = P.ops[o];
-      switch (op.type) {
-        case OP_SIGN:
-          if ((xb & (IT)op.mout) == (IT)op.mout) neg ^= op.rmask;
-          break;
-        case OP_DENSE1:
-          fxg_negate<G>(neg, v);
-          neg = 0;
-          fxg_dense1_dispatch<G>(op.a, &P.coef[op.coef], v);
-          break;
-        case OP_DENSE2:
-          fxg_negate<G>(neg, v);
-          neg = 0;
-          fxg_dense2_dispatch<G>(op.a, op.b, &P.coef[op.coef], v);
-          break;
-        case OP_DIAG:
+    fxs_slot<G, S0>(&P.coef[0], v);
+    if constexpr (S1 != 0) {
+      if (P.sign_end[1] > P.sign_end[0]) {
+        const uint32_t m = signs(P.sign_end[0], P.sign_end[1]);
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const IT x = xb | (IT)P.off[r];
-            int idx = 0;
-            for (int i = 0; i < op.k; ++i) idx = (idx << 1) | int((x >> op.gb[i]) & 1);
-            v[r] = fx_mul1(P.coef[op.coef + idx], v[r]);
-          }
-          break;
-        case OP_PHASE:
-#pragma unroll
-          for (int r = 0; r < R; ++r) v[r] = fx_mul1(P.coef[op.coef], v[r]);
-          break;
-        case OP_CUT:
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const IT x = xb | (IT)P.off[r];
-            const int c = min((int)P.cuts[x], (int)op.ncoef - 1);  // a foreign cut table cannot overrun
-            v[r] = fx_mul1(P.coef[op.coef + c], v[r]);
-          }
-          break;
-        default:
-          break;
+        for (int r = 0; r < R; ++r)
+          if ((m >> r) & 1u) v[r] = fx_neg(v[r]);
       }
+      fxs_slot<G, S1>(&P.coef[16], v);
     }
+    const uint32_t m = P.sign_end[2] > P.sign_end[1] ? signs(P.sign_end[1], P.sign_end[2]) : 0u;
 #pragma unroll
-    for (int r = 0; r < R; ++r) P.out[xb | (IT)P.off[r]] = fx_flip(fx_store_amp<M>(v[r], E), (neg >> r) & 1u);
+    for (int r = 0; r < R; ++r) P.out[xb | (IT)P.off[r]] = fx_flip(fx_store_amp<M>(v[r], E), (m >> r) & 1u);
   }
 }
+
+using FxShapeKernel = void (*)(FxShapeParams);
+#define QF_FX_SHAPES(IT)                                                                                    \
+  {                                                                                                        \
+    k_fxshape<1, 10, 0, IT>, k_fxshape<2, 110, 0, IT>, k_fxshape<1, 10, 10, IT>, k_fxshape<2, 11, 10, IT>,       \
+        k_fxshape<2, 11, 110, IT>, k_fxshape<3, 12, 110, IT>, k_fxshape<2, 110, 11, IT>,                         \
+        k_fxshape<2, 110, 10, IT>, k_fxshape<3, 121, 10, IT>, k_fxshape<2, 110, 110, IT>,                        \
+        k_fxshape<3, 121, 120, IT>, k_fxshape<3, 121, 110, IT>, k_fxshape<4, 132, 110, IT>,                      \
+  }
+// the same order as the shape table of group.cu
+static const FxShapeKernel kFxShapes32[] = QF_FX_SHAPES(uint32_t);
+static const FxShapeKernel kFxShapes64[] = QF_FX_SHAPES(int64_t);
+#undef QF_FX_SHAPES
+// register-capped forms of the widest shapes (more resident warps, fewer
+// registers each; qf_set_fx_occupancy)
+#define QF_FX_WIDE(IT, B)                                                                              \
+  { k_fxshape<3, 121, 120, IT, B>, k_fxshape<3, 121, 110, IT, B>, k_fxshape<4, 132, 110, IT, B> }
+static const FxShapeKernel kFxWide32[3][3] = {QF_FX_WIDE(uint32_t, 2), QF_FX_WIDE(uint32_t, 3),
+                                              QF_FX_WIDE(uint32_t, 4)};
+#undef QF_FX_WIDE
+int g_fx_min_blocks = 1;  // CTAs of the widest shape kernels per SM the registers must allow (1..4)
+static const int kFxShapeG[] = {1, 2, 1, 2, 2, 3, 2, 2, 3, 2, 3, 3, 4};
 
 // --------------------------------------------------------------- host ----
 namespace {
@@ -329,11 +480,7 @@ FxKind fx_kind(const HostOp& op) {
       return FXK_ELEM;
     case OP_PHASE:
       return unit_modulus(op.scalar) ? FXK_ELEM : FXK_NATIVE;
-    case OP_CUT:
-      for (const cplx& c : op.table)
-        if (!unit_modulus(c)) return FXK_NATIVE;
-      return FXK_ELEM;
-    default:
+    default:  // dense gates on 3..5 qubits, QAOA cut-table phases
       return FXK_NATIVE;  // dense gates on 3..5 qubits
   }
 }
@@ -345,9 +492,16 @@ int fx_coef_count(const HostOp& op) {
     case OP_MONO: return op.k == 1 ? 4 : 16;
     case OP_DIAG: return 1 << op.k;
     case OP_PHASE: return 1;
-    case OP_CUT: return (int)op.table.size();
   }
   return 0;
+}
+
+std::vector<cplx> dense_matrix(const HostOp& op) {
+  const int D = 1 << op.k;
+  if (op.type != OP_MONO) return op.m;
+  std::vector<cplx> m((size_t)D * D, cplx(0, 0));
+  for (int r = 0; r < D; ++r) m[r * D + op.perm[r]] = op.diag[r];
+  return m;
 }
 
 struct FxBlock {
@@ -356,6 +510,7 @@ struct FxBlock {
   int G = 0;
   bool native = false;  // one op run by the native FP64 kernels
   int ncoef = 0;
+  int shape = -1;       // table shape of a straight-line pass (-1: other kernels)
 };
 
 constexpr int FX_G_MAX = 4;
@@ -363,9 +518,18 @@ constexpr int FX_G_MAX = 4;
 // Greedy passes: element-wise ops join the current pass; a dense op joins
 // while the pass's dense bits stay within gmax; ops the fixed-point kernels
 // do not take close the pass and run alone in native FP64.
+std::vector<FxBlock> fx_split_shapes(std::vector<FxBlock>& blocks, const std::vector<HostOp>& ops);
+
 std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
   if (fusion_k <= 0) fusion_k = FX_G_MAX;
   if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
+  // generalised permutations on <= 2 qubits with unit-modulus entries run as
+  // dense gates here (one code path for the fixed-point passes)
+  for (HostOp& op : ops)
+    if (op.type == OP_MONO && fx_kind(op) == FXK_DENSE) {
+      op.m = dense_matrix(op);
+      op.type = op.k == 1 ? OP_DENSE1 : OP_DENSE2;
+    }
   const int gmax = std::min(fusion_k, FX_G_MAX);
   const bool fuse = fusion_k > 1;
   std::vector<FxBlock> blocks;
@@ -389,7 +553,8 @@ std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
     if (kind == FXK_DENSE)
       for (int j = 0; j < op.k; ++j)
         if (std::find(cur.order, cur.order + cur.G, op.gb[j]) == cur.order + cur.G) add[nadd++] = op.gb[j];
-    const bool fits = cur.G + nadd <= gmax && (int)cur.idx.size() < FXG_MAX_OPS && cur.ncoef + need <= FXG_MAX_COEF;
+    const bool fits = cur.G + nadd <= gmax && (int)cur.idx.size() < FXG_MAX_OPS / 3 &&
+                      cur.ncoef + need <= FXG_MAX_COEF;
     if (!cur.idx.empty() && (!fuse || !fits)) close();
     if (kind == FXK_DENSE) {
       for (int j = 0; j < op.k; ++j)
@@ -399,7 +564,52 @@ std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
     cur.ncoef += need;
   }
   close();
-  return blocks;
+  return fx_split_shapes(blocks, ops);
+}
+
+// Passes made of dense gates and signs only are cut where their next dense
+// gate would leave the shape table, so each piece runs straight-line.
+std::vector<FxBlock> fx_split_shapes(std::vector<FxBlock>& blocks, const std::vector<HostOp>& ops) {
+  std::vector<FxBlock> out;
+  out.reserve(blocks.size());
+  for (FxBlock& b : blocks) {
+    bool ok = !b.native && b.G > 0;
+    for (int i : b.idx) {
+      const uint8_t t = ops[i].type;
+      ok = ok && (t == OP_DENSE1 || t == OP_DENSE2 || t == OP_SIGN);
+    }
+    if (!ok) {
+      out.push_back(std::move(b));
+      continue;
+    }
+    FxBlock cur;
+    int dense[3], nd = 0;
+    auto finish = [&]() {
+      if (cur.idx.empty()) return;
+      int order[4], G = 0, s0 = 0, s1 = 0;
+      bool swap[2];
+      cur.shape = shape_lookup(ops, dense, nd, order, G, swap, &s0, &s1);
+      cur.G = G;
+      for (int k = 0; k < G; ++k) cur.order[k] = order[k];
+      out.push_back(std::move(cur));
+      cur = FxBlock();
+      nd = 0;
+    };
+    for (int i : b.idx) {
+      if (ops[i].type != OP_SIGN) {
+        if (nd > 0) {
+          int order[4], G = 0, s0 = 0, s1 = 0;
+          bool swap[2];
+          dense[nd] = i;
+          if (nd == 2 || shape_lookup(ops, dense, nd + 1, order, G, swap, &s0, &s1) < 0) finish();
+        }
+        dense[nd++] = i;
+      }
+      cur.idx.push_back(i);
+    }
+    finish();
+  }
+  return out;
 }
 
 int grid_cap(int64_t items) {
@@ -410,13 +620,6 @@ int grid_cap(int64_t items) {
   return (int)g;
 }
 
-std::vector<cplx> dense_matrix(const HostOp& op) {
-  const int D = 1 << op.k;
-  if (op.type != OP_MONO) return op.m;
-  std::vector<cplx> m((size_t)D * D, cplx(0, 0));
-  for (int r = 0; r < D; ++r) m[r * D + op.perm[r]] = op.diag[r];
-  return m;
-}
 
 int launch_fx_single(const void* in, void* out, int n, const HostOp& op, cudaStream_t stream) {
   const double2* src = reinterpret_cast<const double2*>(in);
@@ -443,67 +646,109 @@ int launch_fx_single(const void* in, void* out, int n, const HostOp& op, cudaStr
   return check_cuda(cudaGetLastError());
 }
 
-// Fill the group parameters of block B (its dense bits become register bits:
-// the first-used bit is the top register bit).
+// Fill the group parameters of block B: its dense bits are the register
+// bits, placed so that the first dense gate needs no exchange; before every
+// later dense gate the exchanges that bring its bits to the canonical
+// register bits are emitted, and the host follows the register <-> global
+// bit map through them (element-wise ops and the store use the map in force
+// at their point of the program).
 int fx_group_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, FxGroupParams& P) {
   const int G = B.G;
-  if (n - G < 0 || (int)B.idx.size() > FXG_MAX_OPS) return QF_ERR_NOT_SUPPORTED;
+  if (n - G < 0 || (int)B.idx.size() * 3 > FXG_MAX_OPS) return QF_ERR_NOT_SUPPORTED;
   std::memset(&P, 0, sizeof(FxGroupParams));
   P.n = n;
-  int reg_of[64];
-  std::fill(reg_of, reg_of + 64, -1);
-  int rbits[4] = {0, 0, 0, 0};
-  uint64_t gmask = 0;
-  for (int k = 0; k < G; ++k) {
-    rbits[G - 1 - k] = B.order[k];
-    reg_of[B.order[k]] = G - 1 - k;
-    gmask |= uint64_t(1) << B.order[k];
+  int pos[4] = {0, 0, 0, 0};  // global bit held by register-index bit j
+  {
+    int first = -1;
+    for (int i : B.idx)
+      if (fx_kind(ops[i]) == FXK_DENSE) {
+        first = i;
+        break;
+      }
+    int placed = 0;
+    auto place = [&](int bit) {
+      for (int j = G - placed; j < G; ++j)
+        if (pos[j] == bit) return;
+      pos[G - 1 - placed] = bit;
+      ++placed;
+    };
+    if (first >= 0)
+      for (int j = 0; j < ops[first].k; ++j) place(ops[first].gb[j]);
+    for (int k = 0; k < G; ++k) place(B.order[k]);
   }
+  auto reg_of = [&](int bit) {
+    for (int j = 0; j < G; ++j)
+      if (pos[j] == bit) return j;
+    return -1;
+  };
+  auto offsets = [&](int64_t* off) {
+    for (int r = 0; r < (1 << G); ++r) {
+      int64_t o = 0;
+      for (int j = 0; j < G; ++j)
+        if ((r >> j) & 1) o |= int64_t(1) << pos[j];
+      off[r] = o;
+    }
+  };
+  uint64_t gmask = 0;
   int sb[4];
-  for (int j = 0; j < G; ++j) sb[j] = rbits[j];
+  for (int j = 0; j < G; ++j) {
+    gmask |= uint64_t(1) << pos[j];
+    sb[j] = pos[j];
+  }
   std::sort(sb, sb + G);
   for (int j = 0; j < G; ++j) P.sbits[j] = (uint8_t)sb[j];
-  for (int r = 0; r < (1 << G); ++r) {
-    int64_t o = 0;
-    for (int j = 0; j < G; ++j)
-      if ((r >> j) & 1) o |= int64_t(1) << rbits[j];
-    P.off[r] = o;
-  }
+  offsets(P.off_in);
   int nc = 0, no = 0;
   auto put = [&](cplx v) { P.coef[nc++] = make_fxc(v.real(), v.imag()); };
+  auto swap_to = [&](int j, int target) {
+    if (j == target) return;
+    FxGroupOp& g = P.ops[no++];
+    g.type = FXI_SWAP;
+    g.a = (uint8_t)std::min(j, target);
+    g.b = (uint8_t)std::max(j, target);
+    std::swap(pos[j], pos[target]);
+  };
   for (int i : B.idx) {
     const HostOp& op = ops[i];
-    FxGroupOp& g = P.ops[no++];
     const int need = fx_coef_count(op);
-    if (nc + need > FXG_MAX_COEF) return QF_ERR_NOT_SUPPORTED;
-    g.coef = (uint16_t)nc;
-    const bool dense = op.type == OP_DENSE1 || op.type == OP_DENSE2 || op.type == OP_MONO;
-    if (dense) {
+    if (nc + need > FXG_MAX_COEF || no + 3 > FXG_MAX_OPS) return QF_ERR_NOT_SUPPORTED;
+    if (fx_kind(op) == FXK_DENSE) {
       const std::vector<cplx> m = dense_matrix(op);
       if (op.k == 1) {
-        g.type = OP_DENSE1;
-        g.a = (uint8_t)reg_of[op.gb[0]];
+        swap_to(reg_of(op.gb[0]), G - 1);
+        FxGroupOp& g = P.ops[no++];
+        g.type = FXI_DENSE1;
+        g.coef = (uint16_t)nc;
         for (int e = 0; e < 4; ++e) put(m[e]);
       } else {
-        g.type = OP_DENSE2;
-        const int ja = reg_of[op.gb[0]], jb = reg_of[op.gb[1]];
-        const bool swap = ja < jb;
-        g.a = (uint8_t)(swap ? jb : ja);
-        g.b = (uint8_t)(swap ? ja : jb);
+        // matrix MSB on the top register bit, or (matrix qubits exchanged)
+        // its LSB: whichever needs fewer exchanges
+        const int jm = reg_of(op.gb[0]), jl = reg_of(op.gb[1]);
+        const int cost_a = (jm != G - 1) + (jl != G - 2), cost_b = (jl != G - 1) + (jm != G - 2);
+        const bool exch = cost_b < cost_a;
+        const int top = exch ? op.gb[1] : op.gb[0], second = exch ? op.gb[0] : op.gb[1];
+        swap_to(reg_of(top), G - 1);
+        swap_to(reg_of(second), G - 2);
+        FxGroupOp& g = P.ops[no++];
+        g.type = FXI_DENSE2;
+        g.coef = (uint16_t)nc;
         auto sw = [](int x) { return ((x & 1) << 1) | (x >> 1); };  // exchange the two index bits
         for (int r = 0; r < 4; ++r)
-          for (int c = 0; c < 4; ++c) put(swap ? m[sw(r) * 4 + sw(c)] : m[r * 4 + c]);
+          for (int c = 0; c < 4; ++c) put(exch ? m[sw(r) * 4 + sw(c)] : m[r * 4 + c]);
       }
       continue;
     }
-    g.type = op.type;
+    FxGroupOp& g = P.ops[no++];
+    g.coef = (uint16_t)nc;
     switch (op.type) {
       case OP_SIGN: {
+        g.type = FXI_SIGN;
         uint64_t msk = 0;
         int jm = 0;
         for (int j = 0; j < op.k; ++j) {
           msk |= uint64_t(1) << op.gb[j];
-          if (reg_of[op.gb[j]] >= 0) jm |= 1 << reg_of[op.gb[j]];
+          const int r = reg_of(op.gb[j]);
+          if (r >= 0) jm |= 1 << r;
         }
         g.mout = msk & ~gmask;
         uint32_t rm = 0;
@@ -513,22 +758,23 @@ int fx_group_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, Fx
         break;
       }
       case OP_DIAG:
+        g.type = FXI_DIAG;
         g.k = (uint8_t)op.k;
-        for (int j = 0; j < op.k; ++j) g.gb[j] = (uint8_t)op.gb[j];
+        for (int j = 0; j < op.k; ++j) {
+          g.gb[j] = (uint8_t)op.gb[j];
+          g.rb[j] = (int8_t)reg_of(op.gb[j]);
+        }
         for (int e = 0; e < (1 << op.k); ++e) put(op.diag[e]);
         break;
       case OP_PHASE:
+        g.type = FXI_PHASE;
         put(op.scalar);
-        break;
-      case OP_CUT:
-        g.ncoef = (uint16_t)op.table.size();
-        for (const cplx& c : op.table) put(c);
-        P.cuts = op.cuts;
         break;
       default:
         return QF_ERR_NOT_SUPPORTED;
     }
   }
+  offsets(P.off_out);
   P.nops = no;
   return QF_OK;
 }
@@ -541,17 +787,109 @@ const FxGroupKernel kFxGroup64[5] = {k_fxgroup<0, int64_t>, k_fxgroup<1, int64_t
 
 int fx_group_launch(const FxGroupParams& P, int G, cudaStream_t stream) {
   const int64_t ngroups = int64_t(1) << (P.n - G);
-  (P.n <= 31 ? kFxGroup32 : kFxGroup64)[G]<<<grid_cap(ngroups), 256, 0, stream>>>(P);
+  int64_t grid = (ngroups + FXG_THREADS - 1) / FXG_THREADS;
+  const int64_t cap = (int64_t)device_sm_count() * 16;
+  if (grid > cap) grid = cap;
+  (P.n <= 31 ? kFxGroup32 : kFxGroup64)[G]<<<(int)grid, FXG_THREADS, 0, stream>>>(P);
   return check_cuda(cudaGetLastError());
 }
 
 // kernel used by a block: 0 element-wise group pass, 1 direct sweep,
-// 3 group pass, 5 native FP64 op
+// 3 group pass, 4 shape pass, 5 native FP64 op
 int fx_block_kernel(const std::vector<HostOp>& ops, const FxBlock& B) {
   if (B.native) return 5;
   if (B.G == 0) return 0;
   if (B.idx.size() == 1) return 1;
+  if (B.shape >= 0) return 4;
   return 3;
+}
+
+// Parameters of a shape pass (dense gates and signs; the shape table names
+// the gates' bits in order of first use from the top register bit).
+int fx_shape_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, FxShapeParams& P) {
+  int dense[2], nd = 0, nsign = 0;
+  for (int i : B.idx) {
+    if (ops[i].type == OP_SIGN) {
+      ++nsign;
+    } else {
+      if (nd == 2) return QF_ERR_NOT_SUPPORTED;
+      dense[nd++] = i;
+    }
+  }
+  int order[4], G = 0, s0 = 0, s1 = 0;
+  bool swap[2] = {false, false};
+  const int shape = shape_lookup(ops, dense, nd, order, G, swap, &s0, &s1);
+  if (shape < 0 || nsign > SHAPE_MAX_SIGNS || n - G < 0) return QF_ERR_NOT_SUPPORTED;
+  std::memset(&P, 0, sizeof(FxShapeParams));
+  P.n = n;
+  P.shape = shape;
+  int reg_of[64];
+  std::fill(reg_of, reg_of + 64, -1);
+  uint64_t gmask = 0;
+  int rbits[4];
+  for (int k = 0; k < G; ++k) {
+    rbits[G - 1 - k] = order[k];
+    reg_of[order[k]] = G - 1 - k;
+    gmask |= uint64_t(1) << order[k];
+  }
+  int sb[4];
+  for (int j = 0; j < G; ++j) sb[j] = rbits[j];
+  std::sort(sb, sb + G);
+  for (int j = 0; j < G; ++j) P.sbits[j] = (uint8_t)sb[j];
+  for (int r = 0; r < (1 << G); ++r) {
+    int64_t o = 0;
+    for (int j = 0; j < G; ++j)
+      if ((r >> j) & 1) o |= int64_t(1) << rbits[j];
+    P.off[r] = o;
+  }
+  int slot = 0, ns = 0;
+  for (int i : B.idx) {
+    const HostOp& op = ops[i];
+    if (op.type == OP_SIGN) {
+      uint64_t m = 0;
+      int jm = 0;
+      for (int j = 0; j < op.k; ++j) {
+        m |= uint64_t(1) << op.gb[j];
+        if (reg_of[op.gb[j]] >= 0) jm |= 1 << reg_of[op.gb[j]];
+      }
+      uint32_t rm = 0;
+      for (int r = 0; r < (1 << G); ++r)
+        if ((r & jm) == jm) rm |= 1u << r;
+      P.mout[ns] = m & ~gmask;
+      P.rmask[ns] = (uint16_t)rm;
+      ++ns;
+      continue;
+    }
+    for (int b = slot; b < 3; ++b) P.sign_end[b] = ns;  // a dense slot closes the signs before it
+    FxC* c = &P.coef[16 * slot];
+    if (op.type == OP_DENSE1) {
+      for (int e = 0; e < 4; ++e) c[e] = make_fxc(op.m[e].real(), op.m[e].imag());
+    } else {
+      auto sw = [](int x) { return ((x & 1) << 1) | (x >> 1); };  // exchange the two index bits
+      for (int r = 0; r < 4; ++r)
+        for (int col = 0; col < 4; ++col) {
+          const cplx v = swap[slot] ? op.m[sw(r) * 4 + sw(col)] : op.m[r * 4 + col];
+          c[4 * r + col] = make_fxc(v.real(), v.imag());
+        }
+    }
+    ++slot;
+  }
+  if (nd == 1) P.sign_end[1] = P.sign_end[0];
+  P.sign_end[2] = ns;
+  return QF_OK;
+}
+
+int fx_shape_launch(const FxShapeParams& P, cudaStream_t stream) {
+  const int G = kFxShapeG[P.shape];
+  const int64_t ngroups = int64_t(1) << (P.n - G);
+  int64_t grid = (ngroups + FXS_THREADS - 1) / FXS_THREADS;
+  const int64_t cap = (int64_t)device_sm_count() * 16;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  FxShapeKernel kern = (P.n <= 31 ? kFxShapes32 : kFxShapes64)[P.shape];
+  if (P.n <= 31 && g_fx_min_blocks > 1 && P.shape >= 10) kern = kFxWide32[g_fx_min_blocks - 2][P.shape - 10];
+  kern<<<(int)grid, FXS_THREADS, 0, stream>>>(P);
+  return check_cuda(cudaGetLastError());
 }
 
 }  // namespace
@@ -571,10 +909,20 @@ int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int f
     if (passes_out) *passes_out = passes;
     return QF_OK;
   }
-  static thread_local FxGroupParams gp;  // ~17 KiB: kept off the stack
+  static thread_local FxGroupParams gp;  // ~18 KiB: kept off the stack
+  static thread_local FxShapeParams sp;
   for (FxBlock& B : blocks) {
     int rc;
     switch (fx_block_kernel(ops, B)) {
+      case 4: {
+        rc = fx_shape_prepare(n, ops, B, sp);
+        if (rc) return rc;
+        sp.in = reinterpret_cast<const double2*>(src);
+        sp.out = reinterpret_cast<double2*>(out);
+        LaunchTimer timer(QF_KERNEL_FX_SHAPE, stream);
+        rc = fx_shape_launch(sp, stream);
+        break;
+      }
       case 5: {
         std::vector<HostOp> one(1, ops[B.idx[0]]);
         int p = 0;
@@ -625,8 +973,7 @@ int fx_plan_stats(int n, std::vector<HostOp>& ops, int fusion_k, int32_t* stats,
     uint64_t hm = 0;
     for (int j = 0; j < B.G; ++j) hm |= uint64_t(1) << B.order[j];
     st[6] = __builtin_popcountll(hm & ~uint64_t(31));
-    const int kk = fx_block_kernel(ops, B);
-    st[7] = kk == 0 ? 0 : kk == 1 ? 1 : kk == 3 ? 3 : 5;
+    st[7] = fx_block_kernel(ops, B);
   }
   return QF_OK;
 }

@@ -351,6 +351,15 @@ static int shape_name(const std::vector<HostOp>& ops, const int* dense, int nd, 
 // single-gate sweeps beat it.
 int g_shape_max_bits = 3;
 
+int shape_lookup(const std::vector<HostOp>& ops, const int* dense, int nd, int* order, int& G, bool* swap,
+                 int* s0, int* s1) {
+  const int i = shape_name(ops, dense, nd, order, G, swap);
+  if (i < 0) return -1;
+  *s0 = kShapes[i].s0;
+  *s1 = kShapes[i].s1;
+  return i;
+}
+
 int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd) {
   int order[4], G = 0;
   bool swap[2];

@@ -306,8 +306,8 @@ def test_index_paths_above_2_31_amplitudes(c128, monkeypatch):
     assert nat.lib.qf_plan_circuit(N, layout, nops, op_k.ctypes.data, op_axes.ctypes.data,
                                    op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
     kinds = set(stats[:8 * nb.value].reshape(-1, 8)[:, 7])
-    # lone sweeps and shape passes (float-float) / group passes (fixed point)
-    assert ({1, 4} if c128 == "ff" else {3}) <= kinds
+    # lone sweeps and shape passes (float-float) / shape passes (fixed point)
+    assert ({1, 4} if c128 == "ff" else {4}) <= kinds
     ket = circ.run(qf.zero_state(N))
     assert abs(ket.norm() - 1) < 1e-11
     back = circ.H.run(ket)

@@ -101,3 +101,35 @@ def test_reference_backend_wide_tensormul():
     ref = orc.tensormul(a, b, idx).reshape(-1)
     got = bk.evaluate(out).reshape(-1)
     assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-13
+
+
+@pytest.mark.parametrize("n,k", [(12, 5), (13, 6), (16, 6), (20, 5)])
+def test_tensor_core_dense_gates_c64(n, k):
+    """Dense complex64 gates on 5 and 6 qubits on the tensor cores (tcgen05,
+    split-TF32 operands) against the oracle and against the CUDA-core kernel,
+    out of place and in place, on scattered and on the lowest bits."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(n * 8 + k)
+    st = (rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n))
+    st /= np.linalg.norm(st)
+    u = np.linalg.qr(rng.normal(size=(2 ** k, 2 ** k)) + 1j * rng.normal(size=(2 ** k, 2 ** k)))[0]
+    for axes in ([int(a) for a in rng.choice(n, size=k, replace=False)], list(range(n - k, n))):
+        ref = orc.tensormul(u, st, axes).reshape(-1)
+        scale = np.max(np.abs(ref))
+        tc = _dense(st, u, axes, 0)
+        assert np.max(np.abs(tc - ref)) / scale < 1e-5, axes
+        try:
+            nat.call("qf_set_dense_tensor_cores", 0)
+            cc = _dense(st, u, axes, 0)
+        finally:
+            nat.call("qf_set_dense_tensor_cores", 1)
+        assert np.max(np.abs(tc - cc)) / scale < 1e-5
+        # in place
+        buf = qf.Buffer.from_complex(torch.from_numpy(st.astype(np.complex64)).cuda())
+        dmat = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+        nat.call("qf_apply_dense_gate", nat.ptr(buf.data), nat.ptr(buf.data), n, 0, k, nat.int_array(axes),
+                 nat.ptr(dmat), nat.stream_handle())
+        got = buf.data.cpu().numpy().astype(np.complex128)
+        assert np.max(np.abs(got - ref)) / scale < 1e-5
+    assert nat.device_error() == 0

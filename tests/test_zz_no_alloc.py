@@ -34,11 +34,11 @@ def test_noalloc_matches_workspace_entry_point(layout):
     from quantumflow_gb300 import _native as nat
     tol = 1e-5 if layout == 0 else 1e-12  # relative, as in the other parity tests
     rng = np.random.default_rng(11)
-    # calls in a row with different sizes: n=23 fills the array up to the
+    # calls in a row with different sizes: n=24 fills the array up to the
     # block cap of the reduction (8 blocks per SM), the later ones use fewer
     # blocks, so stale partial sums from the earlier calls sit in the
     # shared array
-    for n, p in ((23, 1), (18, 2), (12, 3), (12, 3)):
+    for n, p in ((24, 1), (18, 2), (12, 3), (12, 3)):
         g = qf.qaoa.random_regular_graph(3, n, seed=n)
         prob = qf.QAOAMaxCut(g, p, dtype="complex64" if layout == 0 else "complex128")
         beta, gamma = rng.uniform(0, np.pi, p), rng.uniform(0, np.pi, p)

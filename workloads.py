@@ -1,22 +1,29 @@
-"""Small reproducible QAOA workloads for timing and profiling.
+"""Small reproducible workloads for timing and profiling (the commands of
+the summaries under profiles/ run these).
 
-    python -m quantumflow_gb300.workloads adjoint --n 24 --p 8 [--dtype complex128] [--reps 2]
+    python workloads.py adjoint --n 24 --p 8 [--dtype complex128] [--reps 2]
         expectation + adjoint gradient of QAOA MAXCUT on a seeded random
         3-regular graph (single instance: k_qaoaw forward, k_adjw adjoint)
-    python -m quantumflow_gb300.workloads batch --count 32 --n 20 --p 6 [--dtype complex64] [--reps 3]
+    python workloads.py batch --count 32 --n 20 --p 6 [--dtype complex64] [--reps 3]
         batched evaluation of `count` seeded random 3-regular instances
         (multi-instance wave passes above the shared-memory tile)
+    python workloads.py layers --n 24 --layers 10 [--arith fx|ff|fp64] [--reps 2]
+        the benchmark's random-layer circuit (bench.py c2_circuit_ops) at a
+        size small enough for a profiler capture
 
 Each prints one line with the mean wall time per evaluation.
 """
 import argparse
+import os
+import sys
 import time
 
 import numpy as np
 import torch
 
-from . import qaoa
-from .batched import QAOABatch
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from quantumflow_gb300 import qaoa  # noqa: E402
+from quantumflow_gb300.batched import QAOABatch  # noqa: E402
 
 
 def adjoint(n: int, p: int, dtype: str = "complex128", reps: int = 2) -> float:
@@ -48,16 +55,36 @@ def batch(count: int, n: int, p: int, dtype: str = "complex64", reps: int = 3) -
     return (time.perf_counter() - t0) / reps
 
 
+def layers(n: int, nlayers: int, arith: str = None, reps: int = 2) -> float:
+    import bench
+    import quantumflow_gb300 as qf
+    if arith:
+        qf.config.C128_ARITHMETIC = arith
+    circ = bench.build_circuit(bench.c2_circuit_ops(n, nlayers, 2018))
+    circ.run(qf.zero_state(n))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        circ.run(qf.zero_state(n))
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("kind", choices=["adjoint", "batch"])
+    ap.add_argument("kind", choices=["adjoint", "batch", "layers"])
+    ap.add_argument("--layers", type=int, default=10)
+    ap.add_argument("--arith", default=None, choices=["fx", "ff", "fp64"])
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--p", type=int, default=8)
     ap.add_argument("--count", type=int, default=32)
     ap.add_argument("--dtype", default=None, choices=["complex64", "complex128"])
     ap.add_argument("--reps", type=int, default=2)
     a = ap.parse_args(argv)
-    if a.kind == "adjoint":
+    if a.kind == "layers":
+        s = layers(a.n, a.layers, a.arith, a.reps)
+        print(f"layers n={a.n} x {a.layers}: {s * 1e3:.3f} ms per circuit")
+    elif a.kind == "adjoint":
         s = adjoint(a.n, a.p, a.dtype or "complex128", a.reps)
         print(f"adjoint n={a.n} p={a.p}: {s * 1e3:.3f} ms per expectation + gradient")
     else:
