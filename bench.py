@@ -79,6 +79,9 @@ KERNEL_TRAFFIC_N24 = {
     "dense2": (268.485120e6, 206.819072e6),
     "warp_tile": (268.507904e6, 207.091712e6),
     "shape": (268.482560e6, 206.890240e6),
+    # fixed-point straight-line pass k_fxshape<4, 132, 110> (mean of 3 launches)
+    "fx_shape": (268.601941e6, 208.636416e6),
+    "fx_group": (268.538240e6, 209.662080e6),
 }
 
 
@@ -231,6 +234,21 @@ def qaoa_time_to_ratio(args):
     for _ in range(reps):
         prob24.expectation_and_grad(b24, g24a)
     grad_rate = reps / (time.perf_counter() - t0)
+    # the same gradient in native FP64 arithmetic (the QAOA kernels compute
+    # complex128 in float-float unless native FP64 is configured)
+    old_arith = qf.config.C128_ARITHMETIC
+    qf.config.C128_ARITHMETIC = "fp64"
+    try:
+        prob64 = qf.QAOAMaxCut(g24, 8)
+        prob64.expectation_and_grad(b24, g24a)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            prob64.expectation_and_grad(b24, g24a)
+        grad_rate_fp64 = reps / (time.perf_counter() - t0)
+        del prob64
+    finally:
+        qf.config.C128_ARITHMETIC = old_arith
     # batched evaluation of 4096 uneven instances (n 10..20, p 1..6; half
     # G(n, 0.5), half random 3-regular where n is even): <C> and adjoint
     # gradient of every instance per evaluation
@@ -268,7 +286,49 @@ def qaoa_time_to_ratio(args):
             "mean_steps_plain": res["plain_single"]["mean_steps"],
             "mean_steps_learned": res["learned_batched"]["mean_steps"],
             "reached": {k: res[k]["reached"] for k in ("plain_single", "plain_batched", "learned_batched")},
-            "adjoint_grad_evals_per_s_n24_p8_c128": grad_rate}
+            "adjoint_grad_evals_per_s_n24_p8_c128": grad_rate,
+            "adjoint_grad_arith": "float-float (48-bit)",
+            "adjoint_grad_evals_per_s_n24_p8_c128_fp64": grad_rate_fp64}
+
+
+def dense_gate_c64(N=26, K=6, reps=5, seed=6):
+    """A dense K-qubit gate (random unitary, scattered axes) on an N-qubit
+    complex64 state through qf_apply_dense_gate: the tcgen05 tensor-core
+    kernel against the CUDA-core kernel, CUDA-event timed on the launch
+    stream (state 8 * 2^N bytes > L2)."""
+    import torch
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(seed)
+    u = np.linalg.qr(rng.normal(size=(2 ** K, 2 ** K)) + 1j * rng.normal(size=(2 ** K, 2 ** K)))[0]
+    axes = [int(a) for a in rng.choice(N, size=K, replace=False)]
+    dmat = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+    psi = torch.zeros(2 ** N, dtype=torch.complex64, device="cuda")
+    psi[0] = 1
+    out = torch.empty_like(psi)
+    stream = torch.cuda.current_stream()
+    res = {}
+    for name, tc in (("tensor_cores", 1), ("cuda_cores", 0)):
+        nat.call("qf_set_dense_tensor_cores", tc)
+        try:
+            def run():
+                nat.call("qf_apply_dense_gate", nat.ptr(psi), nat.ptr(out), N, nat.LAYOUT_C64, K,
+                         nat.int_array(axes), nat.ptr(dmat), nat.stream_handle())
+            run()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                run()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        finally:
+            nat.call("qf_set_dense_tensor_cores", 1)
+        ms = e0.elapsed_time(e1) / reps
+        res[name] = {"ms": ms, "gbs": 2 * 8 * 2 ** N / (ms * 1e-3) / 1e9,
+                     "useful_tflops": 8 * 2 ** K * 2 ** N / (ms * 1e-3) / 1e12}
+    res["tensor_flops_per_useful"] = 3  # hi.hi + hi.lo + lo.hi
+    res["workload"] = f"dense {K}-qubit unitary on a {N}-qubit complex64 state, axes {axes}"
+    return res
 
 
 def max_over_ranks(ms, dist, device):
@@ -332,6 +392,7 @@ def main():
     ap.add_argument("--no-qaoa", action="store_true", help="skip the QAOA time-to-ratio measurement")
     ap.add_argument("--qaoa-graphs", type=int, default=32)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dense", action="store_true", help="skip the wide dense-gate comparison")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--ref-n", type=int, default=28)
     ap.add_argument("--ref-gates", type=int, default=1, help="gates per reference-arm step (CPU sample)")
@@ -484,6 +545,7 @@ def main():
     qaoa = None
     if not args.no_qaoa and rank == 0:
         qaoa = qaoa_time_to_ratio(args)
+    dense = dense_gate_c64() if rank == 0 and not args.no_dense else None
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -516,6 +578,7 @@ def main():
             "sweep_roofline": sweep,
             "kernel_ms_per_step": {k: m / args.steps for k, (m, c) in kt.items() if c},
             "qaoa": qaoa,
+            "dense_gate_c64": dense,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clock_info,

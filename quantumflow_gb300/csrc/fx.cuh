@@ -100,6 +100,16 @@ QF_HD int64_t fx_mad(int32_t a, int32_t b, int64_t c) {
   return static_cast<int64_t>(a) * b + c;
 #endif
 }
+// d = a * b + c, 32x32 -> 64 bits unsigned (one IMAD.WIDE.U32)
+QF_HD uint64_t fx_madu(uint32_t a, uint32_t b, uint64_t c) {
+#ifdef __CUDA_ARCH__
+  uint64_t d;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+#else
+  return static_cast<uint64_t>(a) * b + c;
+#endif
+}
 QF_HD uint32_t fx_hiword(double v) {
 #ifdef __CUDA_ARCH__
   return static_cast<uint32_t>(__double2hiint(v));
@@ -168,7 +178,39 @@ QF_HD double fx_out(int64_t T, int E) {
   const uint32_t s = static_cast<uint32_t>(static_cast<int32_t>(thi) >> 31);
   // |T| as (mh:ml)
   const uint64_t mag = ((static_cast<uint64_t>(thi ^ s) << 32) | (tlo ^ s)) - static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(s)));
-  uint32_t mh = static_cast<uint32_t>(mag >> 32), ml = static_cast<uint32_t>(mag);
+  const uint32_t mh = static_cast<uint32_t>(mag >> 32), ml = static_cast<uint32_t>(mag);
+  // normalise without branches (a branch here would cut the unrolled
+  // conversions of a thread's amplitudes into blocks the scheduler cannot
+  // interleave): lz = leading zeros of the 64-bit |T| (64 when T = 0)
+  const bool big = mh != 0u;
+  const int zh = fx_clz(mh), zl = fx_clz(ml);
+  const int lz = big ? zh : 32 + zl;
+  const uint32_t nh = big ? fx_shl64hi(ml, mh, static_cast<uint32_t>(zh)) : fx_shl64hi(0u, ml, static_cast<uint32_t>(zl));
+  const uint32_t nl = big ? (ml << (zh & 31)) : 0u;
+  // n = |T| << lz has its leading one at bit 63
+  uint32_t qh = nh >> 11;
+  uint32_t ql = fx_shr64lo(nl, nh, 11);
+  const uint32_t rest = nl & 0x7ffu;  // dropped bits; 0x400 is the half
+  const uint32_t inc = (rest > 0x400u || (rest == 0x400u && (ql & 1u))) ? 1u : 0u;
+  const uint64_t q = ((static_cast<uint64_t>(qh) << 32) | ql) + inc;
+  qh = static_cast<uint32_t>(q >> 32);
+  ql = static_cast<uint32_t>(q);
+  const int eb = E + 62 - M - lz;  // biased exponent; the hidden bit of q adds one
+  const uint32_t bits_hi = (qh + (static_cast<uint32_t>(eb - 1) << 20)) | (s & 0x80000000u);
+  const bool zero = (mh | ml) == 0u;
+  return fx_double(zero ? 0u : bits_hi, zero ? 0u : ql);
+}
+
+// The same conversion with a branch on the normalisation: fewer
+// instructions, for kernels that convert only a few values per thread (the
+// single-gate sweeps), where the branch costs no scheduling freedom.
+template <int M>
+QF_HD double fx_out_br(int64_t T, int E) {
+  const uint32_t thi = static_cast<uint32_t>(static_cast<uint64_t>(T) >> 32);
+  const uint32_t tlo = static_cast<uint32_t>(T);
+  const uint32_t s = static_cast<uint32_t>(static_cast<int32_t>(thi) >> 31);
+  const uint64_t mag = ((static_cast<uint64_t>(thi ^ s) << 32) | (tlo ^ s)) - static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(s)));
+  const uint32_t mh = static_cast<uint32_t>(mag >> 32), ml = static_cast<uint32_t>(mag);
   int lz;
   uint32_t nh, nl;
   if (mh != 0u) {
@@ -182,15 +224,14 @@ QF_HD double fx_out(int64_t T, int E) {
     nh = ml << z;
     nl = 0u;
   }
-  // n = |T| << lz has its leading one at bit 63
   uint32_t qh = nh >> 11;
   uint32_t ql = fx_shr64lo(nl, nh, 11);
-  const uint32_t rest = nl & 0x7ffu;  // dropped bits; 0x400 is the half
+  const uint32_t rest = nl & 0x7ffu;
   const uint32_t inc = (rest > 0x400u || (rest == 0x400u && (ql & 1u))) ? 1u : 0u;
   const uint64_t q = ((static_cast<uint64_t>(qh) << 32) | ql) + inc;
   qh = static_cast<uint32_t>(q >> 32);
   ql = static_cast<uint32_t>(q);
-  const int eb = E + 62 - M - lz;  // biased exponent; the hidden bit of q adds one
+  const int eb = E + 62 - M - lz;
   const uint32_t bits_hi = (qh + (static_cast<uint32_t>(eb - 1) << 20)) | (s & 0x80000000u);
   return fx_double(bits_hi, ql);
 }
@@ -208,8 +249,16 @@ struct FxAcc {
     X = fx_mad(ah, cl, X);
     X = fx_mad(al, ch, X);
   }
-  // T = (sum A C) / 2^56, i.e. four times the result in units of A
-  QF_HD int64_t total() const { return H + (X >> FX_L); }
+  // T = (sum A C) / 2^56 = H + floor(X / 2^28), i.e. four times the result
+  // in units of A.  With X = xh 2^32 + xl (xl unsigned), floor(X / 2^28) =
+  // 16 xh + (xl >> 28): two multiply-adds on the IMAD pipe instead of a
+  // 64-bit shift and add on the integer ALU, the busier pipe of these passes.
+  QF_HD int64_t total() const {
+    const int32_t xh = static_cast<int32_t>(static_cast<uint64_t>(X) >> 32);
+    const uint32_t xl = static_cast<uint32_t>(X);
+    const int64_t t = fx_mad(xh, 16, H);
+    return static_cast<int64_t>(fx_madu(xl >> FX_L, 1u, static_cast<uint64_t>(t)));
+  }
 };
 
 // Split a result T (units of A / 4) into the pieces of A = round(T / 4).

@@ -25,16 +25,23 @@
 namespace qf {
 
 // ------------------------------------------------------------- device ----
+// largest FP64 exponent field among the parts of v[]
 template <int R>
-QF_D int fx_group_exp(const double2 (&v)[R]) {
+QF_D int fx_group_exp_raw(const double2 (&v)[R]) {
   uint32_t m = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     m = max(m, fx_hiword(v[r].x) & 0x7fffffffu);
     m = max(m, fx_hiword(v[r].y) & 0x7fffffffu);
   }
-  const int E = static_cast<int>(m >> 20);
-  return E < FX_EMIN ? 4095 : E;  // a group of parts below 2^-959 becomes all zero
+  return static_cast<int>(m >> 20);
+}
+// the group exponent fx_in takes: a group of parts below 2^-959 becomes all
+// zero (an exponent no part reaches shifts every part out)
+QF_D int fx_exp_final(int e) { return e < FX_EMIN ? 4095 : e; }
+template <int R>
+QF_D int fx_group_exp(const double2 (&v)[R]) {
+  return fx_exp_final(fx_group_exp_raw<R>(v));
 }
 
 template <int M>
@@ -87,18 +94,18 @@ __global__ void __launch_bounds__(256) k_fxdense1(const double2* __restrict__ in
       FxAmp f[2] = {fx_load_amp<M>(a[0], E), fx_load_amp<M>(a[1], E)};
       int64_t tr, ti;
       fx_cdot<2>(&u.c[0], f, tr, ti);
-      out[i0] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      out[i0] = make_double2(fx_out_br<M>(tr, E), fx_out_br<M>(ti, E));
       fx_cdot<2>(&u.c[2], f, tr, ti);
-      out[i0 | bit] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      out[i0 | bit] = make_double2(fx_out_br<M>(tr, E), fx_out_br<M>(ti, E));
     }
     if (has2) {
       const int E = fx_group_exp<2>(c);
       FxAmp f[2] = {fx_load_amp<M>(c[0], E), fx_load_amp<M>(c[1], E)};
       int64_t tr, ti;
       fx_cdot<2>(&u.c[0], f, tr, ti);
-      out[j0] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      out[j0] = make_double2(fx_out_br<M>(tr, E), fx_out_br<M>(ti, E));
       fx_cdot<2>(&u.c[2], f, tr, ti);
-      out[j0 | bit] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      out[j0 | bit] = make_double2(fx_out_br<M>(tr, E), fx_out_br<M>(ti, E));
     }
   }
 }
@@ -125,7 +132,7 @@ __global__ void __launch_bounds__(256) k_fxdense2(const double2* __restrict__ in
     for (int r = 0; r < 4; ++r) {
       int64_t tr, ti;
       fx_cdot<4>(&u.c[4 * r], f, tr, ti);
-      out[idx[r]] = make_double2(fx_out<M>(tr, E), fx_out<M>(ti, E));
+      out[idx[r]] = make_double2(fx_out_br<M>(tr, E), fx_out_br<M>(ti, E));
     }
   }
 }
@@ -373,7 +380,44 @@ QF_D void fxs_slot(const FxC* cf, FxAmp (&v)[1 << G]) {
   }
 }
 
-template <int G, int S0, int S1, typename IT, int MINB = 1>
+// the last slot of a pass: results stay as T values (units of A / 4) and are
+// rounded to FP64 straight from there
+template <int G, int J>
+QF_D void fxs_dense1_t(const FxC* cf, const FxAmp (&v)[1 << G], int64_t (&tr)[1 << G], int64_t (&ti)[1 << G]) {
+#pragma unroll
+  for (int i = 0; i < (1 << (G - 1)); ++i) {
+    const int i0 = ((i >> J) << (J + 1)) | (i & ((1 << J) - 1));
+    const int i1 = i0 | (1 << J);
+    const FxAmp p[2] = {v[i0], v[i1]};
+    fx_cdot<2>(cf, p, tr[i0], ti[i0]);
+    fx_cdot<2>(cf + 2, p, tr[i1], ti[i1]);
+  }
+}
+template <int G, int J0, int J1>
+QF_D void fxs_dense2_t(const FxC* cf, const FxAmp (&v)[1 << G], int64_t (&tr)[1 << G], int64_t (&ti)[1 << G]) {
+  constexpr int LO = J0 < J1 ? J0 : J1, HI = J0 < J1 ? J1 : J0;
+#pragma unroll
+  for (int i = 0; i < (1 << (G - 2)); ++i) {
+    int b = ((i >> LO) << (LO + 1)) | (i & ((1 << LO) - 1));
+    b = ((b >> HI) << (HI + 1)) | (b & ((1 << HI) - 1));
+    const int idx[4] = {b, b | (1 << J1), b | (1 << J0), b | (1 << J0) | (1 << J1)};
+    const FxAmp p[4] = {v[idx[0]], v[idx[1]], v[idx[2]], v[idx[3]]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) fx_cdot<4>(cf + 4 * r, p, tr[idx[r]], ti[idx[r]]);
+  }
+}
+template <int G, int S>
+QF_D void fxs_slot_t(const FxC* cf, const FxAmp (&v)[1 << G], int64_t (&tr)[1 << G], int64_t (&ti)[1 << G]) {
+  if constexpr (S >= 100) {
+    fxs_dense2_t<G, (S / 10) % 10, S % 10>(cf, v, tr, ti);
+  } else {
+    fxs_dense1_t<G, S - 10>(cf, v, tr, ti);
+  }
+}
+
+// MINB: resident CTAs per SM the register allocation must allow (narrow
+// shapes need few registers; the widest are tuned by qf_set_fx_occupancy)
+template <int G, int S0, int S1, typename IT, int MINB = (G <= 1 ? 8 : G == 2 ? 4 : 1)>
 __global__ void __launch_bounds__(FXS_THREADS, MINB) k_fxshape(const __grid_constant__ FxShapeParams P) {
   constexpr int R = 1 << G;
   constexpr int M = G <= 2 ? 56 : 55;
@@ -401,19 +445,98 @@ __global__ void __launch_bounds__(FXS_THREADS, MINB) k_fxshape(const __grid_cons
     FxAmp v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = fx_load_amp<M>(a[r], E);
-    fxs_slot<G, S0>(&P.coef[0], v);
+    int64_t tr[R], ti[R];
     if constexpr (S1 != 0) {
+      fxs_slot<G, S0>(&P.coef[0], v);
       if (P.sign_end[1] > P.sign_end[0]) {
         const uint32_t m = signs(P.sign_end[0], P.sign_end[1]);
 #pragma unroll
         for (int r = 0; r < R; ++r)
           if ((m >> r) & 1u) v[r] = fx_neg(v[r]);
       }
-      fxs_slot<G, S1>(&P.coef[16], v);
+      fxs_slot_t<G, S1>(&P.coef[16], v, tr, ti);
+    } else {
+      fxs_slot_t<G, S0>(&P.coef[0], v, tr, ti);
     }
     const uint32_t m = P.sign_end[2] > P.sign_end[1] ? signs(P.sign_end[1], P.sign_end[2]) : 0u;
 #pragma unroll
-    for (int r = 0; r < R; ++r) P.out[xb | (IT)P.off[r]] = fx_flip(fx_store_amp<M>(v[r], E), (m >> r) & 1u);
+    for (int r = 0; r < R; ++r)
+      P.out[xb | (IT)P.off[r]] = fx_flip(make_double2(fx_out<M>(tr[r], E), fx_out<M>(ti[r], E)), (m >> r) & 1u);
+  }
+}
+
+
+// The widest shape (a 4x4 gate on register bits (3,2), then one on (1,0)) on
+// a pair of threads: each holds 8 of the group's 16 amplitudes, so a thread
+// needs about half the registers and twice as many warps fit an SM.  For the
+// first gate a thread holds the amplitudes whose register bit 0 is its half
+// p; the pair then trades four amplitudes through warp shuffles so that for
+// the second gate a thread holds those whose register bit 3 is p.  Both
+// halves use the group's common exponent (a shuffled maximum).  Every lane of
+// a warp runs the same number of iterations (the thread count is a multiple
+// of 32), as the shuffles require.
+template <typename IT>
+__global__ void __launch_bounds__(FXS_THREADS, 3) k_fxpair(const __grid_constant__ FxShapeParams P) {
+  constexpr int M = 55;
+  const IT nitems = IT(2) << (P.n - 4);  // two threads per group
+  const IT nthr = (IT)gridDim.x * blockDim.x;
+  for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < nitems; t += nthr) {
+    const int p = (int)(t & 1);
+    IT xb = t >> 1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) xb = insert0(xb, (int)P.sbits[j]);
+    auto signs = [&](int s0, int s1) {
+      uint32_t m = 0;
+      for (int s = s0; s < s1; ++s)
+        if ((xb & (IT)P.mout[s]) == (IT)P.mout[s]) m ^= P.rmask[s];
+      return m;
+    };
+    // phase 1: local i (bits 3,2,1 of the register) <-> register 2 i + p
+    double2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = P.in[xb | (IT)P.off[2 * i + p]];
+    if (P.sign_end[0] > 0) {
+      const uint32_t m = signs(0, P.sign_end[0]);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a[i] = fx_flip(a[i], (m >> (2 * i + p)) & 1u);
+    }
+    // the exponent of all 16 amplitudes (maximum of the raw exponents first)
+    const int e_own = fx_group_exp_raw<8>(a);
+    const int e_oth = __shfl_xor_sync(0xffffffffu, e_own, 1);
+    const int E = fx_exp_final(e_own > e_oth ? e_own : e_oth);
+    FxAmp v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = fx_load_amp<M>(a[i], E);
+    fxs_dense2<3, 2, 1>(&P.coef[0], v);  // register bits (3,2) are local bits (2,1)
+    if (P.sign_end[1] > P.sign_end[0]) {
+      const uint32_t m = signs(P.sign_end[0], P.sign_end[1]);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if ((m >> (2 * i + p)) & 1u) v[i] = fx_neg(v[i]);
+    }
+    // exchange: keep register bit 3 == p, send bit 3 == !p; phase 2 local j
+    // (bits 2,1,0 of the register) <-> register 8 p + j
+    FxAmp w[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const FxAmp keep = p ? v[4 + k] : v[k];
+      const FxAmp send = p ? v[k] : v[4 + k];
+      FxAmp recv;
+      recv.rh = __shfl_xor_sync(0xffffffffu, send.rh, 1);
+      recv.rl = __shfl_xor_sync(0xffffffffu, send.rl, 1);
+      recv.ih = __shfl_xor_sync(0xffffffffu, send.ih, 1);
+      recv.il = __shfl_xor_sync(0xffffffffu, send.il, 1);
+      w[2 * k] = p ? recv : keep;      // register bit 0 = 0
+      w[2 * k + 1] = p ? keep : recv;  // register bit 0 = 1
+    }
+    int64_t tr[8], ti[8];
+    fxs_dense2_t<3, 1, 0>(&P.coef[16], w, tr, ti);
+    const uint32_t m = P.sign_end[2] > P.sign_end[1] ? signs(P.sign_end[1], P.sign_end[2]) : 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int r = 8 * p + j;
+      P.out[xb | (IT)P.off[r]] = fx_flip(make_double2(fx_out<M>(tr[j], E), fx_out<M>(ti[j], E)), (m >> r) & 1u);
+    }
   }
 }
 
@@ -888,6 +1011,14 @@ int fx_shape_launch(const FxShapeParams& P, cudaStream_t stream) {
   if (grid < 1) grid = 1;
   FxShapeKernel kern = (P.n <= 31 ? kFxShapes32 : kFxShapes64)[P.shape];
   if (P.n <= 31 && g_fx_min_blocks > 1 && P.shape >= 10) kern = kFxWide32[g_fx_min_blocks - 2][P.shape - 10];
+  if (P.shape == 12 && g_fx_min_blocks == 1 && P.n >= 9) {
+    // two threads per group (the thread count, 2^(n-3), is a multiple of 32)
+    int64_t g2 = (int64_t(2) << (P.n - 4)) / FXS_THREADS;
+    if (g2 > cap) g2 = cap;
+    if (g2 < 1) g2 = 1;
+    kern = P.n <= 31 ? k_fxpair<uint32_t> : k_fxpair<int64_t>;
+    grid = g2;
+  }
   kern<<<(int)grid, FXS_THREADS, 0, stream>>>(P);
   return check_cuda(cudaGetLastError());
 }

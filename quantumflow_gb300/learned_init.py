@@ -156,9 +156,11 @@ def time_to_ratio(net, graphs, p=6, target=0.9, max_steps=400, lr=0.05, chunk=10
         batch.optimizer_reset(mc, target)
         done = 0
         ratio, first = batch.optimize(0, lr=lr, reset=False)
+        step = 1  # chunks of 1, 2, 4, ... up to `chunk` steps: few wasted steps past the target
         while (first < 0).any() and done < max_steps:
-            ratio, first = batch.optimize(chunk, lr=lr, reset=False)
-            done += chunk
+            ratio, first = batch.optimize(step, lr=lr, reset=False)
+            done += step
+            step = min(2 * step, chunk)
         dt = time.perf_counter() - t0
         reached = first >= 0
         return {"seconds": dt, "reached": int(reached.sum()),

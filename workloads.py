@@ -10,6 +10,9 @@ the summaries under profiles/ run these).
     python workloads.py layers --n 24 --layers 10 [--arith fx|ff|fp64] [--reps 2]
         the benchmark's random-layer circuit (bench.py c2_circuit_ops) at a
         size small enough for a profiler capture
+    python workloads.py dense --n 22 --k 6 [--reps 2] [--cuda-cores]
+        a dense k-qubit unitary on an n-qubit complex64 state through
+        qf_apply_dense_gate (tensor cores, or the CUDA-core kernel)
 
 Each prints one line with the mean wall time per evaluation.
 """
@@ -70,9 +73,34 @@ def layers(n: int, nlayers: int, arith: str = None, reps: int = 2) -> float:
     return (time.perf_counter() - t0) / reps
 
 
+def dense(n: int, k: int, reps: int = 2, cuda_cores: bool = False) -> float:
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(6)
+    u = np.linalg.qr(rng.normal(size=(2 ** k, 2 ** k)) + 1j * rng.normal(size=(2 ** k, 2 ** k)))[0]
+    axes = [int(a) for a in rng.choice(n, size=k, replace=False)]
+    dmat = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+    psi = torch.zeros(2 ** n, dtype=torch.complex64, device="cuda")
+    psi[0] = 1
+    out = torch.empty_like(psi)
+    nat.call("qf_set_dense_tensor_cores", 0 if cuda_cores else 1)
+
+    def run():
+        nat.call("qf_apply_dense_gate", nat.ptr(psi), nat.ptr(out), n, nat.LAYOUT_C64, k, nat.int_array(axes),
+                 nat.ptr(dmat), nat.stream_handle())
+    run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        run()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("kind", choices=["adjoint", "batch", "layers"])
+    ap.add_argument("kind", choices=["adjoint", "batch", "layers", "dense"])
+    ap.add_argument("--k", type=int, default=6)
+    ap.add_argument("--cuda-cores", action="store_true")
     ap.add_argument("--layers", type=int, default=10)
     ap.add_argument("--arith", default=None, choices=["fx", "ff", "fp64"])
     ap.add_argument("--n", type=int, default=24)
@@ -81,7 +109,10 @@ def main(argv=None):
     ap.add_argument("--dtype", default=None, choices=["complex64", "complex128"])
     ap.add_argument("--reps", type=int, default=2)
     a = ap.parse_args(argv)
-    if a.kind == "layers":
+    if a.kind == "dense":
+        s = dense(a.n, a.k, a.reps, a.cuda_cores)
+        print(f"dense k={a.k} on n={a.n} complex64: {s * 1e3:.3f} ms per gate")
+    elif a.kind == "layers":
         s = layers(a.n, a.layers, a.arith, a.reps)
         print(f"layers n={a.n} x {a.layers}: {s * 1e3:.3f} ms per circuit")
     elif a.kind == "adjoint":
