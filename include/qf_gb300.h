@@ -262,14 +262,18 @@ int qf_batch_qaoa_grad(const qf_batch_instance* instances, int ninstances, int n
  *     once per plan, before any stream capture.
  *   qf_wave_qaoa_grad: one evaluation: out gets, per instance,
  *     dgamma[p], dbeta[p], <C> at out_offset, from the device angle array.
- *     No host synchronisation; may be captured in a CUDA graph. */
+ *     skip: NULL, or a DEVICE array of one int32 per planned instance (plan
+ *     order); a nonzero entry leaves that instance out of the evaluation and
+ *     its outputs at their values from its last evaluation (an optimiser
+ *     that stops instances at a target ratio).  No host synchronisation; may
+ *     be captured in a CUDA graph. */
 int qf_wave_min_qubits(int layout);
 int qf_wave_plan(const qf_batch_instance* instances, int ninstances, int layout, void* host_plan,
                  size_t host_bytes, size_t* host_bytes_needed, size_t* device_bytes_needed);
 int qf_wave_prepare(const void* host_plan, const uint8_t* edges, void* workspace, size_t workspace_bytes,
                     void* stream);
 int qf_wave_qaoa_grad(const void* host_plan, void* workspace, size_t workspace_bytes, const double* angles,
-                      double* out, void* stream);
+                      double* out, const int32_t* skip, void* stream);
 
 /* ------------------------------------------ learned angle initialiser ----- */
 /* A 3-layer message-passing graph network (hidden width 64, FP32) mapping a

@@ -97,7 +97,7 @@ SIGNATURES = {
     "qf_wave_min_qubits": (_c_int, [_c_int]),
     "qf_wave_plan": (_c_int, [_vp, _c_int, _c_int, _vp, _sz, _vp, _vp]),
     "qf_wave_prepare": (_c_int, [_vp, _vp, _vp, _sz, _vp]),
-    "qf_wave_qaoa_grad": (_c_int, [_vp, _vp, _sz, _vp, _vp, _vp]),
+    "qf_wave_qaoa_grad": (_c_int, [_vp, _vp, _sz, _vp, _vp, _vp, _vp]),
     "qf_qaoa_expectation_grad": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _c_int, _dp, _dp, _dp, _c_int,
                                           _vp, _vp, _sz, _vp]),
     "qf_expectation_diag": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _sz, _vp]),

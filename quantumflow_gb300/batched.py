@@ -91,6 +91,9 @@ class QAOABatch:
             esrc[i] = o + 2 * p
         self._gsrc = torch.from_numpy(gsrc).to(self.device)
         self._esrc = torch.from_numpy(esrc).to(self.device)
+        # instance of every angle (masked updates)
+        self._ainst = torch.from_numpy(np.repeat(np.arange(self.count), 2 * self.ps)).to(self.device)
+        self._skip_on = False
         from . import autotune
         cfg = autotune.batch_config(self) if (tile_bits is None or ctas is None) else {}
         self.tile_bits = int(tile_bits if tile_bits is not None else cfg.get("tile_bits", ts_max))
@@ -132,6 +135,9 @@ class QAOABatch:
         # multi-instance passes
         self.nwave = len(waves)
         self._wave_plan = None
+        # plan order is input order: skip[k] leaves instance waves[k] out
+        self._wave_idx = torch.as_tensor(waves, dtype=torch.int64).to(self.device)
+        self._wave_skip = torch.zeros(max(1, self.nwave), dtype=torch.int32, device=self.device)
         if self.nwave:
             winst = (_Instance * self.nwave)(*[self._inst(i) for i in waves])
             hb, db = ctypes.c_size_t(), ctypes.c_size_t()
@@ -179,8 +185,9 @@ class QAOABatch:
                      nat.ptr(self.angles), nat.ptr(self.out), self.layout, self.small_max_n, self.tile_bits,
                      self.ctas, nat.ptr(self.ws), self.ws_bytes, stream)
         if self.nwave:
+            skip = nat.ptr(self._wave_skip) if self._skip_on else None
             nat.call("qf_wave_qaoa_grad", self._wave_plan.ctypes.data, nat.ptr(self.wave_ws), self.wave_ws_bytes,
-                     nat.ptr(self.angles), nat.ptr(self.out), stream)
+                     nat.ptr(self.angles), nat.ptr(self.out), skip, stream)
 
     def expectations(self) -> torch.Tensor:
         """<C> per instance (device tensor, input order) from the last launch."""
@@ -214,10 +221,11 @@ class QAOABatch:
                                                               device=self.device),
             "target": None if target is None else float(target),
         }
+        self._wave_skip.zero_()
         self._graph = None
         self._graph_key = None
 
-    def _opt_step(self, lr, b1, b2, eps):
+    def _opt_step(self, lr, b1, b2, eps, stop=False):
         o = self._opt
         self.launch(nat.stream_handle(self.device))
         if o["mc"] is not None and o["target"] is not None:
@@ -229,10 +237,16 @@ class QAOABatch:
         o["v"].mul_(b2).addcmul_(g, g, value=1 - b2)
         mhat = o["m"] / (1 - b1 ** o["t"])
         vhat = o["v"] / (1 - b2 ** o["t"])
-        self.angles.add_(lr * mhat / (vhat.sqrt() + eps))
+        step = lr * mhat / (vhat.sqrt() + eps)
+        if stop:
+            # instances at the target keep their angles and leave the passes
+            live = o["first"] < 0
+            step = torch.where(live[self._ainst], step, torch.zeros_like(step))
+            self._wave_skip[:self.nwave].copy_((~live[self._wave_idx]).to(torch.int32))
+        self.angles.add_(step)
 
     def optimize(self, steps, lr=0.05, betas=(0.9, 0.999), eps=1e-8, maxcut=None, target=None,
-                 use_graph=True, reset=True):
+                 use_graph=True, reset=True, stop_at_target=False):
         """Gradient ascent on every instance's <C> with Adam, entirely on the
         device: each step is one batched forward + adjoint launch and the
         update, replayed from a CUDA graph.  ``reset=False`` continues the
@@ -241,33 +255,45 @@ class QAOABatch:
         With ``maxcut`` (per instance, input order) and ``target`` the step at
         which each instance first has <C>/maxcut >= target is recorded (-1 if
         never; the ratio is that of the angles a step starts from).  Returns
-        (ratios or <C> at the final angles, first_step)."""
+        (ratios or <C> at the final angles, first_step).
+
+        ``stop_at_target=True`` (needs maxcut and target) also stops each
+        instance once it reaches the target: its angles stay where they
+        reached it and its multi-instance passes are skipped, so a batch costs
+        the steps each instance needs rather than the slowest one's."""
         if reset or getattr(self, "_opt", None) is None:
             self.optimizer_reset(maxcut, target)
+        if stop_at_target and (self._opt["mc"] is None or self._opt["target"] is None):
+            raise ValueError("stop_at_target needs maxcut and target")
         b1, b2 = betas
-        key = (float(lr), b1, b2, eps)
-        if steps > 0:
-            if not use_graph:
-                for _ in range(steps):
-                    self._opt_step(lr, b1, b2, eps)
-            else:
-                done = 0
-                if self._graph is None or self._graph_key != key:
-                    self._opt_step(lr, b1, b2, eps)  # outside capture: sets attributes, caches
-                    done = 1
-                    torch.cuda.synchronize(self.device)
-                    graph = torch.cuda.CUDAGraph()
-                    s = torch.cuda.Stream(self.device)
-                    s.wait_stream(torch.cuda.current_stream(self.device))
-                    with torch.cuda.stream(s):
-                        with torch.cuda.graph(graph, stream=s):
-                            self._opt_step(lr, b1, b2, eps)  # recorded, not run
-                    torch.cuda.current_stream(self.device).wait_stream(s)
-                    self._graph, self._graph_key = graph, key
-                for _ in range(steps - done):
-                    self._graph.replay()
-        o = self._opt
-        self.launch()
+        stop = bool(stop_at_target)
+        key = (float(lr), b1, b2, eps, stop)
+        self._skip_on = stop
+        try:
+            if steps > 0:
+                if not use_graph:
+                    for _ in range(steps):
+                        self._opt_step(lr, b1, b2, eps, stop)
+                else:
+                    done = 0
+                    if self._graph is None or self._graph_key != key:
+                        self._opt_step(lr, b1, b2, eps, stop)  # outside capture: sets attributes, caches
+                        done = 1
+                        torch.cuda.synchronize(self.device)
+                        graph = torch.cuda.CUDAGraph()
+                        s = torch.cuda.Stream(self.device)
+                        s.wait_stream(torch.cuda.current_stream(self.device))
+                        with torch.cuda.stream(s):
+                            with torch.cuda.graph(graph, stream=s):
+                                self._opt_step(lr, b1, b2, eps, stop)  # recorded, not run
+                        torch.cuda.current_stream(self.device).wait_stream(s)
+                        self._graph, self._graph_key = graph, key
+                    for _ in range(steps - done):
+                        self._graph.replay()
+            o = self._opt
+            self.launch()
+        finally:
+            self._skip_on = False
         e = self.out[self._esrc]
         first = o["first"]
         if o["mc"] is not None and o["target"] is not None:

@@ -37,7 +37,7 @@ int wave_plan(const qf_batch_instance* hinst, int ninst, int layout, void* host_
               size_t* need_host, size_t* need_device);
 int wave_prepare(const void* host_plan, const uint8_t* edges, void* ws, size_t ws_bytes, cudaStream_t stream);
 int wave_run(const void* host_plan, void* ws, size_t ws_bytes, const double* angles, double* out,
-             cudaStream_t stream);
+             const int32_t* skip, cudaStream_t stream);
 }  // namespace qf
 
 using namespace qf;
@@ -322,11 +322,11 @@ int qf_wave_prepare(const void* host_plan, const uint8_t* edges, void* workspace
 }
 
 int qf_wave_qaoa_grad(const void* host_plan, void* workspace, size_t workspace_bytes, const double* angles,
-                      double* out, void* stream) {
+                      double* out, const int32_t* skip, void* stream) {
   if (host_plan == nullptr || angles == nullptr || out == nullptr) return QF_ERR_INVALID_ARGUMENT;
   if (workspace == nullptr) return QF_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0) return QF_ERR_ALIGNMENT;
-  return wave_run(host_plan, workspace, workspace_bytes, angles, out, as_stream(stream));
+  return wave_run(host_plan, workspace, workspace_bytes, angles, out, skip, as_stream(stream));
 }
 
 size_t qf_batch_workspace_bytes(int max_n, int layout, int ctas) {

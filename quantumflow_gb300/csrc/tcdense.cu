@@ -21,11 +21,17 @@
 // caller's complex128 device matrix) and a two-stage ring of X chunks (hi and
 // lo), all in the canonical K-major layout with 128-byte swizzling: row r of
 // a 32-element chunk is 128 bytes at r * 128, its 16-byte pieces permuted by
-// XOR with (r mod 8); groups of 8 rows are 1024 bytes apart.  Threads gather
-// the X chunk of the next stage while the tensor cores consume the current
-// one; one thread issues the MMAs and commits them to an mbarrier.  Every
-// wait is bounded (4 s); on expiry the kernel raises the device error word
-// and stops.
+// XOR with (r mod 8); groups of 8 rows are 1024 bytes apart.  Two threads
+// share a tile row (8 amplitudes of each chunk apiece) and hold the whole
+// next tile of their row in registers: the loads of tile t+1's chunk c are
+// issued as soon as chunk c of tile t is in shared memory, so one tile of
+// reads (64 KB at K = 6) is in flight per SM while the tensor cores work.
+// One thread issues the MMAs and commits them to the stage's mbarrier.  The
+// accumulators alternate between two tensor-memory regions by tile, so the
+// epilogue of tile t (tcgen05.ld, scattered stores) runs while the MMAs of
+// tile t+1's first chunk execute.  Every wait is bounded (4 s); on expiry the
+// kernel raises the device error word and stops, with every thread leaving
+// the loop at the same barrier (__syncthreads_or of the failures).
 #include <algorithm>
 #include <atomic>
 #include <cstring>
@@ -39,8 +45,9 @@ int* device_error_word();
 namespace {
 
 constexpr int TC_M = 128;        // column groups per tile (MMA M)
-constexpr int TC_THREADS = 128;  // one thread per tile row
+constexpr int TC_THREADS = 256;  // two threads per tile row
 constexpr int TC_KC = 32;        // K elements per chunk (128 bytes of fp32)
+constexpr int TC_AH = TC_KC / 4; // amplitudes per thread per chunk
 
 struct TcParams {
   const float2* in;
@@ -138,28 +145,29 @@ template <int K>
 struct TcGeom {
   static constexpr int D = 1 << K;          // amplitudes per column group
   static constexpr int KD = 2 * D;          // real width (GEMM K and N)
-  static constexpr int NCH = KD / TC_KC;    // K chunks
+  static constexpr int NCH = KD / TC_KC;    // K chunks (2 or 4: even, so stage = chunk parity)
   static constexpr uint32_t B_CHUNK = KD * 128;        // one 32-wide chunk of the gate: N rows x 128 B
   static constexpr uint32_t B_BYTES = NCH * B_CHUNK;   // one plane (hi or lo)
   static constexpr uint32_t A_CHUNK = TC_M * 128;      // one 32-wide chunk of X: 128 rows x 128 B
   // layout: B hi | B lo | A stage 0 hi | A stage 0 lo | A stage 1 hi | A stage 1 lo
   static constexpr uint32_t A_OFF = 2 * B_BYTES;
   static constexpr uint32_t BYTES = A_OFF + 4 * A_CHUNK;
-  static constexpr int TMEM_COLS = KD < 32 ? 32 : KD;  // fp32 accumulator columns
+  static constexpr int TMEM_COLS = 2 * KD;  // two fp32 accumulators (by tile parity)
 };
 
 template <int K>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tcdense(const __grid_constant__ TcParams P) {
   using Geo = TcGeom<K>;
   constexpr int D = Geo::D, KD = Geo::KD, NCH = Geo::NCH;
+  static_assert(NCH % 2 == 0, "the stage of a chunk is its parity within the tile");
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   // 1024-byte alignment of the swizzled regions
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int64_t offs[D];
-  __shared__ int stop;
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (TC_M - 1), half = tid >> 7;
 
   for (int c = tid; c < D; c += TC_THREADS) {
     int64_t o = 0;
@@ -169,18 +177,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tcdense(const __grid_constant
   }
   // the gate's real form, hi and lo planes: B row n = output real n, column
   // k = input real k (Gr[2r][2c] = Re, [2r][2c+1] = -Im, [2r+1][2c] = Im,
-  // [2r+1][2c+1] = Re of G[r][c])
-  for (int e = tid; e < KD * KD; e += TC_THREADS) {
-    const int nrow = e / KD, kcol = e % KD;
-    const double2 g = P.mat[(nrow >> 1) * D + (kcol >> 1)];
-    double v;
-    if ((nrow & 1) == 0) v = (kcol & 1) == 0 ? g.x : -g.y;
-    else v = (kcol & 1) == 0 ? g.y : g.x;
-    const float f = static_cast<float>(v);
-    const float h = tc_hi(f);
-    const uint32_t off = (kcol / TC_KC) * Geo::B_CHUNK + tc_swz(nrow, kcol % TC_KC);
-    *reinterpret_cast<float*>(sm + off) = h;
-    *reinterpret_cast<float*>(sm + Geo::B_BYTES + off) = f - h;
+  // [2r+1][2c+1] = Re of G[r][c]); one complex entry per iteration
+  for (int e = tid; e < D * D; e += TC_THREADS) {
+    const double2 g = P.mat[e];
+    const int r = e >> K, c = e & (D - 1);
+    const float re = static_cast<float>(g.x), im = static_cast<float>(g.y);
+    const uint32_t chunk = static_cast<uint32_t>((2 * c) / TC_KC) * Geo::B_CHUNK;
+    const uint32_t o0 = chunk + tc_swz(2 * r, (2 * c) % TC_KC), o1 = chunk + tc_swz(2 * r + 1, (2 * c) % TC_KC);
+    const float2 h0 = make_float2(tc_hi(re), tc_hi(-im)), h1 = make_float2(tc_hi(im), tc_hi(re));
+    *reinterpret_cast<float2*>(sm + o0) = h0;
+    *reinterpret_cast<float2*>(sm + o1) = h1;
+    *reinterpret_cast<float2*>(sm + Geo::B_BYTES + o0) = make_float2(re - h0.x, -im - h0.y);
+    *reinterpret_cast<float2*>(sm + Geo::B_BYTES + o1) = make_float2(im - h1.x, re - h1.y);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&tmem_slot)),
@@ -192,7 +200,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tcdense(const __grid_constant
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar[0])) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar[1])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    stop = 0;
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
@@ -201,40 +208,80 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tcdense(const __grid_constant
   const uint32_t tmem = tmem_slot;
   const uint32_t idesc = tc_idesc(KD);
   const uint32_t sbase = tc_smem(sm);
+  // this thread's TMEM lanes (its warp's quarter of the rows) and output columns
+  const uint32_t lane_addr = static_cast<uint32_t>(32 * (warp & 3)) << 16;
   uint32_t phase = 0u;    // bit s: the parity stage s's next wait expects
   uint32_t pending = 0u;  // bit s: a commit on stage s not yet waited for
+  int fail = 0;           // this thread saw a wait expire
 
   const int64_t ngroups = int64_t(1) << (P.n - K);
   const int64_t ntiles = ngroups / TC_M;  // the host launches only when TC_M divides ngroups
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // this thread's column group
-    int64_t b = tile * TC_M + tid;
+  auto row_base = [&](int64_t tile) {
+    int64_t b = tile * TC_M + row;
     for (int j = 0; j < K; ++j) b = insert0(b, P.sbits[j]);
+    return b;
+  };
+  // stores the accumulator of a finished tile (rows of base b) to the output
+  auto epilogue = [&](int64_t b, uint32_t acc) {
+#pragma unroll
+    for (int c0 = 0; c0 < KD / 2; c0 += 32) {
+      float v[32];
+      tc_ld32(acc + lane_addr + static_cast<uint32_t>(half * (KD / 2) + c0), v);
+      const int a0 = (half * (KD / 2) + c0) / 2;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) P.out[b | offs[a0 + i]] = make_float2(v[2 * i], v[2 * i + 1]);
+    }
+  };
+
+  // registers: this thread's 8 amplitudes of every chunk of its row's next tile
+  float2 x[NCH][TC_AH];
+  int64_t tile = blockIdx.x;
+  int64_t cur_b = 0, prev_b = 0;
+  if (tile < ntiles) {
+    cur_b = row_base(tile);
+#pragma unroll
+    for (int kc = 0; kc < NCH; ++kc)
+#pragma unroll
+      for (int j = 0; j < TC_AH; ++j) x[kc][j] = P.in[cur_b | offs[kc * (TC_KC / 2) + half * TC_AH + j]];
+  }
+  int it = 0;
+  bool stopped = false;
+  for (; tile < ntiles && !stopped; tile += gridDim.x, ++it) {
+    const bool has_next = tile + gridDim.x < ntiles;
+    const int64_t nb = has_next ? row_base(tile + gridDim.x) : 0;
+    const uint32_t acc = tmem + static_cast<uint32_t>((it & 1) * KD);
+#pragma unroll
     for (int kc = 0; kc < NCH; ++kc) {
       const int s = kc & 1;
       // the MMAs that last read this stage must be done before it is rewritten
       if ((pending >> s) & 1u) {
-        if (!tc_wait(&bar[s], (phase >> s) & 1u, P.err)) stop = 1;
+        if (!tc_wait(&bar[s], (phase >> s) & 1u, P.err)) fail = 1;
         phase ^= 1u << s;
         pending &= ~(1u << s);
       }
-      // gather 16 amplitudes (32 reals) of this thread's group into row
-      // tid, two amplitudes (one 16-byte piece) at a time
+      // split this thread's amplitudes of chunk kc into the stage's hi and lo
+      // rows, two amplitudes (one 16-byte piece) at a time
       unsigned char* ahi = sm + Geo::A_OFF + (2 * s) * Geo::A_CHUNK;
       unsigned char* alo = ahi + Geo::A_CHUNK;
 #pragma unroll
-      for (int c = 0; c < TC_KC / 2; c += 2) {
-        const float2 v0 = P.in[b | offs[kc * (TC_KC / 2) + c]];
-        const float2 v1 = P.in[b | offs[kc * (TC_KC / 2) + c + 1]];
+      for (int j = 0; j < TC_AH; j += 2) {
+        const float2 v0 = x[kc][j], v1 = x[kc][j + 1];
         const float4 h = make_float4(tc_hi(v0.x), tc_hi(v0.y), tc_hi(v1.x), tc_hi(v1.y));
-        const uint32_t o = tc_swz(tid, 2 * c);
+        const uint32_t o = tc_swz(row, 2 * (half * TC_AH + j));
         *reinterpret_cast<float4*>(ahi + o) = h;
         *reinterpret_cast<float4*>(alo + o) = make_float4(v0.x - h.x, v0.y - h.y, v1.x - h.z, v1.y - h.w);
       }
+      // the same chunk of the next tile: in flight until this chunk comes round again
+      if (has_next) {
+#pragma unroll
+        for (int j = 0; j < TC_AH; ++j) x[kc][j] = P.in[nb | offs[kc * (TC_KC / 2) + half * TC_AH + j]];
+      }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tc_fence_before();
-      __syncthreads();
-      if (stop) break;
+      if (__syncthreads_or(fail)) {
+        stopped = true;
+        break;
+      }
       tc_fence_after();
       if (tid == 0) {
         const uint32_t a_hi = sbase + Geo::A_OFF + (2 * s) * Geo::A_CHUNK, a_lo = a_hi + Geo::A_CHUNK;
@@ -242,40 +289,37 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tcdense(const __grid_constant
 #pragma unroll
         for (int ks = 0; ks < TC_KC / 8; ++ks) {  // 8 tf32 (32 bytes) per MMA
           const uint32_t koff = ks * 32;
-          const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-          tc_mma(tmem, tc_desc(a_hi + koff), tc_desc(b_hi + koff), idesc, acc);
-          tc_mma(tmem, tc_desc(a_hi + koff), tc_desc(b_lo + koff), idesc, 1u);
-          tc_mma(tmem, tc_desc(a_lo + koff), tc_desc(b_hi + koff), idesc, 1u);
+          const uint32_t accumulate = (kc > 0 || ks > 0) ? 1u : 0u;
+          tc_mma(acc, tc_desc(a_hi + koff), tc_desc(b_hi + koff), idesc, accumulate);
+          tc_mma(acc, tc_desc(a_hi + koff), tc_desc(b_lo + koff), idesc, 1u);
+          tc_mma(acc, tc_desc(a_lo + koff), tc_desc(b_hi + koff), idesc, 1u);
         }
         tc_commit(&bar[s]);
       }
       pending |= 1u << s;
+      if (kc == 0 && it > 0) {
+        // the previous tile: the commit of its last chunk (stage 1) covers
+        // all of its MMAs; its accumulator is read while this tile's first
+        // chunk is on the tensor cores
+        if (!tc_wait(&bar[1], (phase >> 1) & 1u, P.err)) fail = 1;
+        phase ^= 2u;
+        pending &= ~2u;
+        if (__all_sync(0xffffffffu, fail == 0)) epilogue(prev_b, tmem + static_cast<uint32_t>(((it - 1) & 1) * KD));
+      }
     }
-    if (stop) break;
-    // the last commit covers every MMA of the tile
-    const int sl = (NCH - 1) & 1;
-    if (!tc_wait(&bar[sl], (phase >> sl) & 1u, P.err)) stop = 1;
-    phase ^= 1u << sl;
-    pending &= ~(1u << sl);
-    __syncthreads();
-    if (stop) break;
-    tc_fence_after();
-    // epilogue: TMEM lane (32 warp + lane) = this thread's group; column n =
-    // output real n
-#pragma unroll
-    for (int c0 = 0; c0 < KD; c0 += 32) {
-      float v[32];
-      tc_ld32(tmem + (static_cast<uint32_t>(32 * warp) << 16) + c0, v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) P.out[b | offs[c0 / 2 + i]] = make_float2(v[2 * i], v[2 * i + 1]);
-    }
-    tc_fence_before();
-    __syncthreads();  // every warp has read TMEM before the next tile's MMAs overwrite it
-    tc_fence_after();
+    prev_b = cur_b;
+    cur_b = nb;
   }
-  // drain: MMAs still reading shared memory must finish before the CTA exits
+  // drain: MMAs still reading shared memory or writing tensor memory finish
+  // before the last tile's epilogue and the CTA's exit
   for (int s = 0; s < 2; ++s)
-    if ((pending >> s) & 1u) tc_wait(&bar[s], (phase >> s) & 1u, P.err);
+    if ((pending >> s) & 1u) {
+      if (!tc_wait(&bar[s], (phase >> s) & 1u, P.err)) fail = 1;
+    }
+  tc_fence_before();
+  const int any_fail = __syncthreads_or(fail);
+  tc_fence_after();
+  if (!stopped && !any_fail && it > 0) epilogue(prev_b, tmem + static_cast<uint32_t>(((it - 1) & 1) * KD));
   tc_fence_before();
   __syncthreads();
   if (warp == 0)

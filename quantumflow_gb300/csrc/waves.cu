@@ -93,9 +93,9 @@ __global__ void k_wave_cuts(const WvInst* inst, int ninst, const uint8_t* edges,
 
 // angle-dependent tables of every instance (once per evaluation)
 template <int LAY>
-__global__ void k_wave_coefs(const WvInst* inst, int ninst, const double* angles, Coef* tab) {
+__global__ void k_wave_coefs(const WvInst* inst, int ninst, const double* angles, Coef* tab, const int32_t* skip) {
   const int i = blockIdx.x;
-  if (i >= ninst) return;
+  if (i >= ninst || (skip != nullptr && skip[i] != 0)) return;
   const WvInst I = inst[i];
   const double* beta = angles + I.angle_offset;
   const double* gamma = beta + I.p;
@@ -164,7 +164,8 @@ constexpr size_t wv_ring_bytes(int vectors) {
 // ------------------------------------------------------------- forward ----
 template <int LAY, int RB>
 __global__ void __launch_bounds__(256) k_wave_fwd(const WvFwd* items, int nitems, const WvInst* inst, void* states,
-                                                  const uint16_t* cuts, const Coef* tab, int cutb) {
+                                                  const uint16_t* cuts, const Coef* tab, int cutb,
+                                                  const int32_t* skip) {
   using E = typename Types<LAY>::E;
   constexpr int R = 1 << RB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -175,6 +176,8 @@ __global__ void __launch_bounds__(256) k_wave_fwd(const WvFwd* items, int nitems
     s_in = inst[s_it.inst];
   }
   __syncthreads();
+  // a skipped instance keeps its states and partial rows from its last evaluation
+  if (skip != nullptr && skip[s_it.inst] != 0) return;
   const WvFwd& F = s_it;
   const WvInst& I = s_in;
   const int E1 = I.nedges + 1;
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(256) k_wave_fwd(const WvFwd* items, int nitems
 template <int LAY, int RB>
 __global__ void __launch_bounds__(256) k_wave_adj(const WvAdj* items, int nitems, const WvInst* inst, void* states,
                                                   const uint16_t* cuts, const Coef* tab, double* partials,
-                                                  int cutb) {
+                                                  int cutb, const int32_t* skip) {
   using E = typename Types<LAY>::E;
   constexpr int R = 1 << RB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -269,6 +272,7 @@ __global__ void __launch_bounds__(256) k_wave_adj(const WvAdj* items, int nitems
     s_in = inst[s_it.inst];
   }
   __syncthreads();
+  if (skip != nullptr && skip[s_it.inst] != 0) return;
   const WvAdj& A = s_it;
   const WvInst& I = s_in;
   const int E1 = I.nedges + 1;
@@ -789,7 +793,8 @@ int wave_prepare(const void* host_plan, const uint8_t* edges, void* ws, size_t w
 }
 
 template <int LAY, int RBF, int RBA>
-static int wave_run_t(const PlanView& v, char* d, const double* angles, double* out, cudaStream_t stream) {
+static int wave_run_t(const PlanView& v, char* d, const double* angles, double* out, const int32_t* skip,
+                      cudaStream_t stream) {
   const WvPlanHeader& h = *v.h;
   const WvInst* dinst = reinterpret_cast<const WvInst*>(d + h.off_inst);
   const Coef* dtab = reinterpret_cast<const Coef*>(d + h.off_tab);
@@ -813,7 +818,7 @@ static int wave_run_t(const PlanView& v, char* d, const double* angles, double* 
     if (rc) return rc;
     attr[dev].store(true);
   }
-  k_wave_coefs<LAY><<<h.ninst, 128, 0, stream>>>(dinst, h.ninst, angles, const_cast<Coef*>(dtab));
+  k_wave_coefs<LAY><<<h.ninst, 128, 0, stream>>>(dinst, h.ninst, angles, const_cast<Coef*>(dtab), skip);
   int rc = check_cuda(cudaGetLastError());
   if (rc) return rc;
   const WvFwd* dfwd = reinterpret_cast<const WvFwd*>(d + h.off_fwd);
@@ -822,12 +827,12 @@ static int wave_run_t(const PlanView& v, char* d, const double* angles, double* 
     const WvWave& W = v.waves[w];
     if (W.fwd_count > 0) {
       k_wave_fwd<LAY, RBF><<<W.fwd_blocks, 256, smem_f, stream>>>(
-          dfwd + W.fwd_begin, W.fwd_count, dinst, dstates, dcuts, dtab, (int)cutb);
+          dfwd + W.fwd_begin, W.fwd_count, dinst, dstates, dcuts, dtab, (int)cutb, skip);
       if ((rc = check_cuda(cudaGetLastError()))) return rc;
     }
     if (W.adj_count > 0) {
       k_wave_adj<LAY, RBA><<<W.adj_blocks, 256, smem_a, stream>>>(
-          dadj + W.adj_begin, W.adj_count, dinst, dstates, dcuts, dtab, dpart, (int)cutb);
+          dadj + W.adj_begin, W.adj_count, dinst, dstates, dcuts, dtab, dpart, (int)cutb, skip);
       if ((rc = check_cuda(cudaGetLastError()))) return rc;
     }
   }
@@ -841,13 +846,13 @@ static int wave_run_t(const PlanView& v, char* d, const double* angles, double* 
 }
 
 int wave_run(const void* host_plan, void* ws, size_t ws_bytes, const double* angles, double* out,
-             cudaStream_t stream) {
+             const int32_t* skip, cudaStream_t stream) {
   PlanView v;
   if (!view_plan(host_plan, v)) return QF_ERR_INVALID_ARGUMENT;
   if (ws_bytes < (size_t)v.h->device_bytes) return QF_ERR_WORKSPACE;
   char* d = reinterpret_cast<char*>(ws);
-  if (v.h->layout == C64) return wave_run_t<C64, 4, 3>(v, d, angles, out, stream);
-  if (v.h->layout == FF) return wave_run_t<FF, 3, 2>(v, d, angles, out, stream);
+  if (v.h->layout == C64) return wave_run_t<C64, 4, 3>(v, d, angles, out, skip, stream);
+  if (v.h->layout == FF) return wave_run_t<FF, 3, 2>(v, d, angles, out, skip, stream);
   return QF_ERR_LAYOUT;
 }
 

@@ -155,10 +155,11 @@ def time_to_ratio(net, graphs, p=6, target=0.9, max_steps=400, lr=0.05, chunk=10
         batch.set_angles(betas, gammas)
         batch.optimizer_reset(mc, target)
         done = 0
-        ratio, first = batch.optimize(0, lr=lr, reset=False)
+        ratio, first = batch.optimize(0, lr=lr, reset=False, stop_at_target=True)
         step = 1  # chunks of 1, 2, 4, ... up to `chunk` steps: few wasted steps past the target
         while (first < 0).any() and done < max_steps:
-            ratio, first = batch.optimize(step, lr=lr, reset=False)
+            # each instance stops at the target, as the one-at-a-time loop does
+            ratio, first = batch.optimize(step, lr=lr, reset=False, stop_at_target=True)
             done += step
             step = min(2 * step, chunk)
         dt = time.perf_counter() - t0

@@ -155,6 +155,42 @@ def test_batch_adam_graph_replay_improves_all():
     np.testing.assert_allclose(e2, e1, rtol=1e-5, atol=1e-5)
 
 
+def test_batch_stop_at_target_skips_finished_instances():
+    """optimize(stop_at_target=True) freezes each instance at the step it
+    reaches the target and leaves it out of the multi-instance passes: the
+    first-hit steps equal those of the unmasked run, the instances that never
+    reach the target follow bit-identical trajectories, and the stopped ones
+    report a ratio at or above the target."""
+    import quantumflow_gb300 as qf
+    from quantumflow_gb300 import learned_init as li
+    graphs, ps, rng = _mixed_instances(12, 17, nmin=10, nmax=17, pmax=3)
+    mc = li.max_cuts(graphs)
+    betas = [np.full(p, 0.3) for p in ps]
+    gammas = [np.full(p, 0.4) for p in ps]
+
+    def run(target, stop, use_graph=True):
+        batch = qf.batched.QAOABatch(graphs, ps, dtype="complex64")
+        assert batch.nwave > 0 and batch.nsmall > 0
+        batch.set_angles(betas, gammas)
+        ratio, first = batch.optimize(0, maxcut=mc, target=target, reset=True, stop_at_target=stop)
+        for steps in (1, 2, 4, 5):
+            ratio, first = batch.optimize(steps, lr=0.05, reset=False, stop_at_target=stop, use_graph=use_graph)
+        return ratio, first
+
+    # a target that splits the batch: the median ratio the unmasked run ends at
+    r_free, _ = run(2.0, False)
+    target = float(np.median(r_free))
+    r0, f0 = run(target, False)
+    r1, f1 = run(target, True)
+    r2, f2 = run(target, True, use_graph=False)
+    assert np.array_equal(f0, f1) and np.array_equal(f1, f2)
+    done = f1 >= 0
+    assert done.any() and (~done).any()
+    assert np.all(r1[done] >= target)
+    assert np.array_equal(r0[~done], r1[~done])
+    np.testing.assert_allclose(r2, r1, rtol=1e-6, atol=1e-6)
+
+
 def test_batch_malformed_instance_is_skipped():
     import ctypes
     import quantumflow_gb300 as qf

@@ -103,7 +103,7 @@ def test_reference_backend_wide_tensormul():
     assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-13
 
 
-@pytest.mark.parametrize("n,k", [(12, 5), (13, 6), (16, 6), (20, 5)])
+@pytest.mark.parametrize("n,k", [(12, 5), (13, 6), (16, 6), (20, 5), (22, 6)])
 def test_tensor_core_dense_gates_c64(n, k):
     """Dense complex64 gates on 5 and 6 qubits on the tensor cores (tcgen05,
     split-TF32 operands) against the oracle and against the CUDA-core kernel,
