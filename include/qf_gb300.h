@@ -112,7 +112,10 @@ int qf_set_tile_kernel(int mode);
  * process-wide (tuning; no reference counterpart).  A fused pass of dense
  * gates and CZ-like signs is cut into straight-line shape kernels of at
  * most this many gate bits each; 0 = no shape passes (fused passes stay
- * whole and run the interpreted group or warp-tile kernels). */
+ * whole and run the interpreted group or warp-tile kernels).  Complex64
+ * passes that form one table shape (one or two dense gates on at most four
+ * bits, with signs) run as shape kernels unless this is 0; they are never
+ * cut. */
 int qf_set_shape_bits(int bits);
 /* Gate merging before pass planning (diagnostics and tests; no reference
  * counterpart), process-wide, whenever fusion_k > 1: 1 (default) =

@@ -718,14 +718,14 @@ QF_D void lswap_dispatch(int l, int j, int lane, E (&a)[1 << RB]) {
 }
 
 template <int RB, typename E>
-QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t xb,
-                      const int64_t (&hoff)[1 << RB], E (&a)[1 << RB]) {
+QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, int64_t base, int64_t lx, int lane,
+                      uint32_t pb, E (&a)[1 << RB]) {
   constexpr int R = 1 << RB;
-  // Sign ops (CZ-like) first, as one parity mask over the registers: the
-  // part of a mask outside the register bits is tested once per thread,
-  // only register bits per register (all ops of a segment are diagonal and
-  // commute, so the signs can be applied last).
-  const int64_t regbits = hoff[R - 1];
+  // Sign ops (CZ-like) as one parity mask over the registers, from the
+  // host's resolution of each op against the sub-tile layout (tile bits
+  // tested on the base, lane bits on the lane, register bits as a register
+  // mask); all ops of a segment are diagonal and commute, so the signs are
+  // applied last.
   uint32_t negmask = 0;
   bool other = false;
   for (int o = in.a; o < in.a + in.b; ++o) {
@@ -734,21 +734,23 @@ QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, 
       other = true;
       continue;
     }
-    const uint64_t m = so.mask, mreg = m & (uint64_t)regbits, mout = m & ~mreg;
-    if (((uint64_t)xb & mout) != mout) continue;
-    if (mreg == 0) {
-      negmask ^= (1u << R) - 1u;
-    } else {
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        if (((uint64_t)hoff[r] & mreg) == mreg) negmask ^= 1u << r;
-    }
+    if (((uint64_t)base & so.tmask) == so.tmask && ((uint32_t)lane & so.lmask) == so.lmask) negmask ^= so.rmask;
   }
+  if (other) {
+    // register r holds global index base | lx | hoff[r]
+    int64_t hoff[R];
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int64_t x = xb | hoff[r];
-    E v = a[r];
-    if (other) {
+    for (int r = 0; r < R; ++r) {
+      int64_t o = 0;
+#pragma unroll
+      for (int j = 0; j < RB; ++j)
+        if ((r >> j) & 1) o |= int64_t(1) << ((pb >> (8 * j)) & 255u);
+      hoff[r] = o;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int64_t x = base | lx | hoff[r];
+      E v = a[r];
       for (int o = in.a; o < in.a + in.b; ++o) {
         const SegOp& so = P.segs[o];
         switch (so.type) {
@@ -770,8 +772,13 @@ QF_D void seg_apply_w(const WarpParams& P, const TInstr& in, const Coef* scoef, 
             break;
         }
       }
+      a[r] = v;
     }
-    a[r] = ((negmask >> r) & 1u) ? cneg(v) : v;
+  }
+  if (negmask != 0) {
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      if ((negmask >> r) & 1u) a[r] = cneg(a[r]);
   }
 }
 
@@ -840,13 +847,6 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
     uint32_t pb = pb0;
     uint64_t lm = 0x0403020100ull;
     int64_t lx = lane;
-    auto offset = [&](int r) {
-      int64_t o = 0;
-#pragma unroll
-      for (int j = 0; j < RB; ++j)
-        if ((r >> j) & 1) o |= int64_t(1) << ((pb >> (8 * j)) & 255u);
-      return o;
-    };
     E a[R];
     {
       const E* sp = ring + (size_t)sg * R * 32 + lane;
@@ -873,21 +873,16 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
             g2_reg_dispatch<RB>(in.a, in.b, &P.coef[in.coef], a);
           }
           break;
-        case I_RSWAP:
-          if constexpr (SWAP) {
-            rswap_dispatch<RB>(in.a, in.b, a);
-            const uint32_t sa = 8u * in.a, sb = 8u * in.b;
-            const uint32_t va = (pb >> sa) & 255u, vb = (pb >> sb) & 255u;
-            pb = (pb & ~((255u << sa) | (255u << sb))) | (vb << sa) | (va << sb);
-          }
-          break;
-        case I_SEG: {
-          int64_t hoff[R];
-#pragma unroll
-          for (int r = 0; r < R; ++r) hoff[r] = offset(r);
-          seg_apply_w<RB>(P, in, scoef, base | lx, hoff, a);
+        case I_RSWAP: {
+          rswap_dispatch<RB>(in.a, in.b, a);
+          const uint32_t sa = 8u * in.a, sb = 8u * in.b;
+          const uint32_t va = (pb >> sa) & 255u, vb = (pb >> sb) & 255u;
+          pb = (pb & ~((255u << sa) | (255u << sb))) | (vb << sa) | (va << sb);
           break;
         }
+        case I_SEG:
+          seg_apply_w<RB>(P, in, scoef, base, lx, lane, pb, a);
+          break;
         case I_LSWAP: {
           lswap_dispatch<RB>(in.a, in.b, lane, a);
           const uint32_t sl = 8u * in.a, sj = 8u * in.b;
@@ -899,9 +894,10 @@ __global__ void __launch_bounds__(256) k_warp(const __grid_constant__ WarpParams
         }
       }
     }
-    // the program ends with every lane bit back on its own global bit
+    // the program ends with every lane and register bit back on its own
+    // global bit: the stores reuse the prefetch offsets
 #pragma unroll
-    for (int r = 0; r < R; ++r) gout[base | lane | offset(r)] = a[r];
+    for (int r = 0; r < R; ++r) gout[base | lane | hoff0[r]] = a[r];
   }
   cp_async_wait<0>();
 }
@@ -1561,6 +1557,18 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
       }
       so.coef = (uint16_t)coef_at[i];
       so.ncoef = (uint16_t)coef_count(op);
+      if (op.type == OP_SIGN) {
+        // where the op's bits are at this point of the program
+        uint32_t jm = 0;
+        for (int j = 0; j < op.k; ++j) {
+          const int g = op.gb[j], p = reg_pos(g), l = lane_pos(g);
+          if (p >= 0) jm |= 1u << p;
+          else if (l >= 0) so.lmask |= (uint8_t)(1u << l);
+          else so.tmask |= uint64_t(1) << g;
+        }
+        for (int r = 0; r < (1 << RB); ++r)
+          if ((r & jm) == jm) so.rmask |= (uint16_t)(1u << r);
+      }
       if (nprog > 0 && P.prog[nprog - 1].code == I_SEG && P.prog[nprog - 1].b < 255 &&
           P.prog[nprog - 1].a + P.prog[nprog - 1].b == nseg) {
         P.prog[nprog - 1].b++;
@@ -1597,6 +1605,12 @@ static int launch_warp_t(const void* in, void* out, int n, const std::vector<Hos
     if (lanes[l] == l) continue;
     if (reg_pos(l) < 0) lswap(lane_pos(l), SWAP ? RB - 1 : 0);
     lswap(l, reg_pos(l));
+  }
+  // and the register bits (register moves), so that the stores use the
+  // offsets of the loads
+  for (int j = 0; j < RB && ok; ++j) {
+    const int p = reg_pos(hb[j]);
+    if (p != j) rswap(p, j);
   }
   if (!ok) return QF_ERR_NOT_SUPPORTED;
   P.nprog = nprog;
@@ -1907,7 +1921,11 @@ struct PlanBlock {
 // of 2x2 gates and CZs at N=26 ran 23.7 ms split against 29.9 ms on warp
 // tiles and 119.3 against 114.6 ms per 10 merged random layers at N=28 when
 // such passes stayed whole).  Blocks with other ops stay whole.
-static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<HostOp>& ops) {
+// max_chunks > 0: a block that would become more shape passes than this
+// stays whole (complex64: a state sweep per shape pass costs more than one
+// interpreted warp-tile pass of many gates).
+static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<HostOp>& ops, int max_bits,
+                             int max_chunks) {
   std::vector<PlanBlock> out;
   out.reserve(blocks.size());
   for (PlanBlock& b : blocks) {
@@ -1920,10 +1938,11 @@ static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<H
       out.push_back(std::move(b));
       continue;
     }
+    std::vector<PlanBlock> chunks;
     PlanBlock cur;
     int dense[3], nd = 0;
     auto close = [&]() {
-      if (!cur.idx.empty()) out.push_back(std::move(cur));
+      if (!cur.idx.empty()) chunks.push_back(std::move(cur));
       cur = PlanBlock();
       nd = 0;
     };
@@ -1931,7 +1950,7 @@ static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<H
       const HostOp& op = ops[i];
       if (op.type != OP_SIGN) {
         dense[nd] = i;
-        if (nd > 0 && (nd == 2 || shape_of(ops, dense, nd + 1) < 0)) {
+        if (nd > 0 && (nd == 2 || shape_of(ops, dense, nd + 1, max_bits) < 0)) {
           close();
           dense[0] = i;
         }
@@ -1943,6 +1962,11 @@ static void split_for_shapes(std::vector<PlanBlock>& blocks, const std::vector<H
       cur.ncoef += coef_count(op);
     }
     close();
+    if (max_chunks > 0 && (int)chunks.size() > max_chunks) {
+      out.push_back(std::move(b));
+      continue;
+    }
+    for (PlanBlock& c : chunks) out.push_back(std::move(c));
   }
   blocks.swap(out);
 }
@@ -1977,7 +2001,12 @@ static std::vector<PlanBlock> plan_blocks(std::vector<HostOp>& ops, int n, int l
     cur.elem_only = cur.elem_only && is_elementwise(op.type);
   }
   if (!cur.idx.empty()) blocks.push_back(cur);
-  if (layout == FF && group_pass_enabled() && g_shape_max_bits > 0) split_for_shapes(blocks, ops);
+  if (layout == FF && group_pass_enabled() && g_shape_max_bits > 0)
+    split_for_shapes(blocks, ops, shape_max_bits(FF), 0);
+  // complex64: a three-gate pass with CZ signs ran 1.55 ms on a warp tile at
+  // N=28 against 0.67 ms per two-gate shape pass
+  if (layout == C64 && group_pass_enabled() && shape_max_bits(C64) > 0)
+    split_for_shapes(blocks, ops, shape_max_bits(C64), 2);
   return blocks;
 }
 

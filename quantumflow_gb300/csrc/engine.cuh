@@ -72,8 +72,14 @@ struct SegOp {
   uint8_t gb[3];
   uint8_t pad[3];
   uint16_t coef, ncoef;  // into the element-wise coefficient table
-  uint32_t pad2;
+  // OP_SIGN in warp-tile programs, resolved by the host against the
+  // sub-tile layout at the op's program point: rmask = the registers whose
+  // index has every register bit of the op set, lmask = the lane bits that
+  // hold op bits, tmask = the op bits in the sub-tile base
+  uint16_t rmask;
+  uint8_t lmask, pad2;
   uint64_t mask;  // OP_SIGN: the k global bits
+  uint64_t tmask;
 };
 // Warp-tile programs (k_warp): a sub-tile is 32 lanes (global bits 0..4)
 // x 2^RB registers (the block's RB high bits hb[]), streamed straight from
@@ -202,19 +208,19 @@ int group_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::
                   GroupParams& P, int& G);
 int group_launch(const GroupParams& P, int G, cudaStream_t stream);
 
-// Shape passes (k_shape, float-float layout): the straight-line form of a
-// group pass for the common programs -- one or two dense gates (slots) on
-// fixed register bits, with sign ops (CZ-like) between and around them as
-// per-thread register masks.  The host renames the pass's gate bits to
-// register bits in order of first use (top first), which maps every
-// program of the table in group.cu to one compiled kernel.
+// Shape passes (k_shape, float-float and complex64 layouts): the
+// straight-line form of a group pass for the common programs -- one or two
+// dense gates (slots) on fixed register bits, with sign ops (CZ-like)
+// between and around them as per-thread register masks.  The host renames
+// the pass's gate bits to register bits in order of first use (top first),
+// which maps every program of the table in group.cu to one compiled kernel.
 constexpr int SHAPE_MAX_SIGNS = 64;
 struct ShapeParams {
   const void* in;
   void* out;
   int32_t n, shape;
   int32_t sign_end[3];  // signs [sign_end[b-1], sign_end[b]) act before slot b (b = 2: after the last)
-  int32_t pad;
+  int32_t layout;       // FF or C64
   uint8_t sbits[4];     // the group bits, ascending
   uint8_t dense[2];     // slot s: every coefficient part nonzero
   uint8_t pad2[2];
@@ -223,10 +229,13 @@ struct ShapeParams {
   uint64_t mout[SHAPE_MAX_SIGNS];
   Coef coef[32];        // slot s at coef[16 s]
 };
-// Which table shape the dense ops ops[dense[0..nd)] form (-1: none); the
-// planner splits fused float-float passes at the points where the next
-// dense gate would leave the table.
-int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd);
+// Which table shape of at most max_bits gate bits the dense ops
+// ops[dense[0..nd)] form (-1: none); the planner splits fused float-float
+// and complex64 passes at the points where the next dense gate would leave
+// the table.
+int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd, int max_bits);
+// Widest shape in gate bits for a layout (0: no shape passes).
+int shape_max_bits(int layout);
 // The table shape of ops[dense[0..nd)] whatever the width limit: returns its
 // index (or -1), the bits in order of first use (order[0] is register bit
 // G-1), G, which 4x4 slots have their matrix MSB on the lower register bit

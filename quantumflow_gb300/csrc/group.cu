@@ -38,7 +38,7 @@ QF_D void group_g2(int a, int b, const Coef* cf, float4 (&v)[1 << G], bool dense
 }
 
 // negate the registers whose bit is set in neg (sign-bit flips on all four
-// float-float words)
+// float-float words, or both words of a complex64 amplitude)
 template <int R>
 QF_D void apply_negmask(uint32_t neg, float4 (&v)[R]) {
 #pragma unroll
@@ -48,6 +48,15 @@ QF_D void apply_negmask(uint32_t neg, float4 (&v)[R]) {
     v[r].y = __uint_as_float(__float_as_uint(v[r].y) ^ s);
     v[r].z = __uint_as_float(__float_as_uint(v[r].z) ^ s);
     v[r].w = __uint_as_float(__float_as_uint(v[r].w) ^ s);
+  }
+}
+template <int R>
+QF_D void apply_negmask(uint32_t neg, float2 (&v)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const uint32_t s = (neg << (31 - r)) & 0x80000000u;
+    v[r].x = __uint_as_float(__float_as_uint(v[r].x) ^ s);
+    v[r].y = __uint_as_float(__float_as_uint(v[r].y) ^ s);
   }
 }
 
@@ -255,8 +264,8 @@ static const ShapeDef kShapes[] = {
 };
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <int G, int S>
-QF_D void slot_apply(const Coef* cf, float4 (&v)[1 << G], bool dense) {
+template <int G, int S, typename E>
+QF_D void slot_apply(const Coef* cf, E (&v)[1 << G], bool dense) {
   if constexpr (S >= 100) {
     g2_reg<G, (S / 10) % 10, S % 10>(cf, v, dense);
   } else if constexpr (S >= 10) {
@@ -264,19 +273,21 @@ QF_D void slot_apply(const Coef* cf, float4 (&v)[1 << G], bool dense) {
   }
 }
 
-// IT: index type (uint32_t for states of at most 2^31 amplitudes)
-template <int G, int S0, int S1, typename IT>
+// LAY: FF (float4 amplitudes) or C64 (float2); IT: index type (uint32_t
+// for states of at most 2^31 amplitudes)
+template <int LAY, int G, int S0, int S1, typename IT>
 __global__ void __launch_bounds__(256) k_shape(const __grid_constant__ ShapeParams P) {
+  using E = typename Types<LAY>::E;
   constexpr int R = 1 << G;
-  const float4* gin = reinterpret_cast<const float4*>(P.in);
-  float4* gout = reinterpret_cast<float4*>(P.out);
+  const E* gin = reinterpret_cast<const E*>(P.in);
+  E* gout = reinterpret_cast<E*>(P.out);
   const IT ngroups = IT(1) << (P.n - G);
   const IT nthr = (IT)gridDim.x * blockDim.x;
   for (IT t = (IT)blockIdx.x * blockDim.x + threadIdx.x; t < ngroups; t += nthr) {
     IT xb = t;
 #pragma unroll
     for (int j = 0; j < G; ++j) xb = insert0(xb, P.sbits[j]);
-    float4 v[R];
+    E v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = gin[xb | (IT)P.off[r]];
     auto signs = [&](int s0, int s1) {
@@ -298,15 +309,18 @@ __global__ void __launch_bounds__(256) k_shape(const __grid_constant__ ShapePara
 }
 
 using ShapeKernel = void (*)(ShapeParams);
-#define QF_SHAPES(IT)                                                                                 \
-  {                                                                                                  \
-    k_shape<1, 10, 0, IT>, k_shape<2, 110, 0, IT>, k_shape<1, 10, 10, IT>, k_shape<2, 11, 10, IT>,       \
-        k_shape<2, 11, 110, IT>, k_shape<3, 12, 110, IT>, k_shape<2, 110, 11, IT>,                     \
-        k_shape<2, 110, 10, IT>, k_shape<3, 121, 10, IT>, k_shape<2, 110, 110, IT>,                    \
-        k_shape<3, 121, 120, IT>, k_shape<3, 121, 110, IT>, k_shape<4, 132, 110, IT>,                  \
+#define QF_SHAPES(L, IT)                                                                                \
+  {                                                                                                    \
+    k_shape<L, 1, 10, 0, IT>, k_shape<L, 2, 110, 0, IT>, k_shape<L, 1, 10, 10, IT>,                      \
+        k_shape<L, 2, 11, 10, IT>, k_shape<L, 2, 11, 110, IT>, k_shape<L, 3, 12, 110, IT>,               \
+        k_shape<L, 2, 110, 11, IT>, k_shape<L, 2, 110, 10, IT>, k_shape<L, 3, 121, 10, IT>,              \
+        k_shape<L, 2, 110, 110, IT>, k_shape<L, 3, 121, 120, IT>, k_shape<L, 3, 121, 110, IT>,           \
+        k_shape<L, 4, 132, 110, IT>,                                                                   \
   }
-static const ShapeKernel kShapeKernels32[kNumShapes] = QF_SHAPES(uint32_t);
-static const ShapeKernel kShapeKernels64[kNumShapes] = QF_SHAPES(int64_t);
+static const ShapeKernel kShapeKernelsFF32[kNumShapes] = QF_SHAPES(FF, uint32_t);
+static const ShapeKernel kShapeKernelsFF64[kNumShapes] = QF_SHAPES(FF, int64_t);
+static const ShapeKernel kShapeKernelsC64_32[kNumShapes] = QF_SHAPES(C64, uint32_t);
+static const ShapeKernel kShapeKernelsC64_64[kNumShapes] = QF_SHAPES(C64, int64_t);
 #undef QF_SHAPES
 
 // Register naming of a dense-op program: bits in order of first use get
@@ -360,16 +374,23 @@ int shape_lookup(const std::vector<HostOp>& ops, const int* dense, int nd, int* 
   return i;
 }
 
-int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd) {
+int shape_of(const std::vector<HostOp>& ops, const int* dense, int nd, int max_bits) {
   int order[4], G = 0;
   bool swap[2];
   const int s = shape_name(ops, dense, nd, order, G, swap);
-  return G <= g_shape_max_bits ? s : -1;
+  return G <= max_bits ? s : -1;
 }
+
+// Complex64 passes take every shape of the table: their FP32 bodies are a
+// quarter of the float-float ones (the four-bit two-4x4 shape is short), and
+// a pass that moves the state once for two gates is what an HBM-bound
+// layout wants.  Measured at N=28 (100 random layers): 342.7 ms per step on
+// warp tiles alone.  qf_set_shape_bits(0) turns shape passes off for both.
+int shape_max_bits(int layout) { return layout == C64 && g_shape_max_bits > 0 ? 4 : g_shape_max_bits; }
 
 int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::vector<int>& idx,
                   ShapeParams& P) {
-  if (layout != FF) return QF_ERR_NOT_SUPPORTED;
+  if (layout != FF && layout != C64) return QF_ERR_NOT_SUPPORTED;
   int dense[2], nd = 0, nsign = 0;
   for (int i : idx) {
     const HostOp& op = ops[i];
@@ -385,10 +406,11 @@ int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::
   int order[4], G = 0;
   bool swap[2] = {false, false};
   const int shape = shape_name(ops, dense, nd, order, G, swap);
-  if (shape < 0 || G > g_shape_max_bits || nsign > SHAPE_MAX_SIGNS || n - G < 8) return QF_ERR_NOT_SUPPORTED;
+  if (shape < 0 || G > shape_max_bits(layout) || nsign > SHAPE_MAX_SIGNS || n - G < 8) return QF_ERR_NOT_SUPPORTED;
   std::memset(&P, 0, sizeof(ShapeParams));
   P.n = n;
   P.shape = shape;
+  P.layout = layout;
   int reg_of[64];
   std::fill(reg_of, reg_of + 64, -1);
   uint64_t gmask = 0;
@@ -428,7 +450,7 @@ int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::
     for (int b = slot; b < 3; ++b) P.sign_end[b] = ns;
     Coef* c = &P.coef[16 * slot];
     if (op.type == OP_DENSE1) {
-      for (int e = 0; e < 4; ++e) c[e] = make_coef(op.m[e], FF);
+      for (int e = 0; e < 4; ++e) c[e] = make_coef(op.m[e], layout);
     } else {
       bool all = true;
       for (int e = 0; e < 16; ++e) all = all && op.m[e].real() != 0.0 && op.m[e].imag() != 0.0;
@@ -436,7 +458,7 @@ int shape_prepare(int n, int layout, const std::vector<HostOp>& ops, const std::
       auto sw = [](int x) { return ((x & 1) << 1) | (x >> 1); };  // exchange the two index bits
       for (int r = 0; r < 4; ++r)
         for (int col = 0; col < 4; ++col)
-          c[4 * r + col] = make_coef(swap[slot] ? op.m[sw(r) * 4 + sw(col)] : op.m[r * 4 + col], FF);
+          c[4 * r + col] = make_coef(swap[slot] ? op.m[sw(r) * 4 + sw(col)] : op.m[r * 4 + col], layout);
     }
     ++slot;
   }
@@ -455,7 +477,9 @@ int shape_launch(const ShapeParams& P, cudaStream_t stream) {
   const int64_t cap = (int64_t)device_sm_count() * 8;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  (P.n <= 31 ? kShapeKernels32 : kShapeKernels64)[P.shape]<<<(int)grid, 256, 0, stream>>>(P);
+  const ShapeKernel* table = P.layout == C64 ? (P.n <= 31 ? kShapeKernelsC64_32 : kShapeKernelsC64_64)
+                                             : (P.n <= 31 ? kShapeKernelsFF32 : kShapeKernelsFF64);
+  table[P.shape]<<<(int)grid, 256, 0, stream>>>(P);
   return check_cuda(cudaGetLastError());
 }
 
