@@ -56,12 +56,11 @@ QF_D double2 fx_store_amp(const FxAmp& a, int E) {
   return make_double2(fx_out<M>(fx_t_of(a.rh, a.rl), E), fx_out<M>(fx_t_of(a.ih, a.il), E));
 }
 // flip the FP64 sign of both parts (a pending CZ-like sign at store time)
+// as an integer XOR of the sign bits: a floating-point negation can take the
+// FP64 pipe, a few lanes per clock on this part
 QF_D double2 fx_flip(double2 v, bool neg) {
-  if (neg) {
-    v.x = -v.x;
-    v.y = -v.y;
-  }
-  return v;
+  const uint32_t s = neg ? 0x80000000u : 0u;
+  return make_double2(fx_double(fx_hiword(v.x) ^ s, fx_loword(v.x)), fx_double(fx_hiword(v.y) ^ s, fx_loword(v.y)));
 }
 
 struct FxCoef4 {
