@@ -486,11 +486,11 @@ def main():
         torch.cuda.synchronize()
         nat.timing_enable(False)
         sk = nat.timing_collect()
-        kind = "fx_dense1" if sk["fx_dense1"][1] else "dense1"
+        kind = next((k for k in ("fx_dense1", "fx_tensor", "dense1") if sk[k][1]), "dense1")
         sms, scount = sk[kind]
         if scount:
             sweep_ach = sweep_bytes / (sms / scount * 1e-3) / 1e9
-            kname = "k_fxdense1" if kind == "fx_dense1" else "k_dense1"
+            kname = {"fx_dense1": "k_fxdense1", "fx_tensor": "k_txpipe", "dense1": "k_dense1"}[kind]
             sweep = {"kernel": f"{kname} (one 2x2 gate per pass, all {N} qubits)", "achieved": sweep_ach,
                      "peak": None, "unit": "GB/s", "frac": None, "launches_timed": scount}
 
@@ -561,8 +561,8 @@ def main():
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"fx": "c128 (FP64 storage; int64 fixed-point gate arithmetic, >= 55-bit, "
-                            "one FP64 rounding per pass)",
+            "dtype": {"fx": "c128 (FP64 storage; fused passes as 61-bit fixed-point integer digits on fp16 "
+                            "tensor-core MMAs with exact FP32 accumulation, one FP64 rounding per pass)",
                       "ff": "c128 (float-float arithmetic)", "fp64": "c128 (FP64)",
                       "fp32": "c64 (FP32)"}[arith],
             "data": "synthetic",

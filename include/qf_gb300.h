@@ -96,7 +96,8 @@ size_t qf_reduce_workspace_bytes(int n);
 #define QF_KERNEL_FX_GROUP 10      /* fixed-point fused pass on a register group  */
 #define QF_KERNEL_FX_ELEMENTWISE 11 /* fixed-point pass of element-wise ops only  */
 #define QF_KERNEL_FX_SHAPE 12      /* fixed-point straight-line pass (1-2 gates)  */
-#define QF_KERNEL_CLASSES 13
+#define QF_KERNEL_FX_TENSOR 13     /* complex128 pass on the tensor cores         */
+#define QF_KERNEL_CLASSES 14
 int qf_timing_enable(int on);
 /* Fused-pass kernel selection (diagnostics and tests; no reference
  * counterpart), process-wide: 0 = default (float-float group passes --
@@ -130,7 +131,7 @@ int qf_set_gate_merging(int on);
  * bit (< 5), element-wise, other, high bits (>= 5), kernel (0 element-wise,
  * 1 direct single-gate sweep, 2 fused warp-tile or shared-memory pass,
  * 3 group pass, 4 shape pass, 5 one gate in native FP64 inside a
- * QF_LAYOUT_FX circuit).  *nblocks gets the pass count; at most max_blocks
+ * QF_LAYOUT_FX circuit, 6 tensor-core complex128 pass).  *nblocks gets the pass count; at most max_blocks
  * rows are written. */
 int qf_plan_circuit(int n, int layout, int nops, const int* op_k, const int* op_axes, const double* op_mats,
                     int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
@@ -175,6 +176,14 @@ int qf_set_dense_tensor_cores(int on);
  * (1..4; the register cap trades per-thread registers for warps), states of
  * at most 2^31 amplitudes.  Process-wide tuning, no reference counterpart. */
 int qf_set_fx_occupancy(int min_blocks);
+/* Complex128 (QF_LAYOUT_FX) fused passes on the tensor cores (default 1):
+ * a pass of unitary gates on at most four bits, with CZ-like signs around
+ * them, runs as one 16 x 16 unitary applied by fp16 tcgen05 MMAs to
+ * base-256 integer digits of a 60-bit fixed-point form of each row of 16
+ * amplitudes (exact FP32 accumulation, one FP64 rounding per pass; states
+ * of at least 2^11 amplitudes); 0 = the CUDA-core fixed-point kernels.
+ * Process-wide; no reference counterpart. */
+int qf_set_fx_tensor_cores(int on);
 
 /* Apply nops gates in order with gate fusion.  Replaces the per-gate loop of
  * quantumflow/circuits.py:87-99 Circuit.run.  Gate i acts on op_k[i] axes

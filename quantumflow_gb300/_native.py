@@ -70,6 +70,7 @@ SIGNATURES = {
     "qf_set_gate_merging": (_c_int, [_c_int]),
     "qf_set_dense_tensor_cores": (_c_int, [_c_int]),
     "qf_set_fx_occupancy": (_c_int, [_c_int]),
+    "qf_set_fx_tensor_cores": (_c_int, [_c_int]),
     "qf_plan_circuit": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_int, _vp]),
     "qf_timing_collect": (_c_int, [_dp, ctypes.POINTER(ctypes.c_int64), _c_int]),
     "qf_sample_workspace_bytes": (_sz, [_c_int]),
@@ -163,7 +164,7 @@ def device_error(stream=None):
 
 
 KERNEL_CLASSES = ("fused_tile", "dense1", "dense2", "permutation", "elementwise", "warp_tile", "group", "shape",
-                  "fx_dense1", "fx_dense2", "fx_group", "fx_elementwise", "fx_shape")
+                  "fx_dense1", "fx_dense2", "fx_group", "fx_elementwise", "fx_shape", "fx_tensor")
 
 
 def timing_enable(on=True):

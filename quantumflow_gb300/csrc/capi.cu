@@ -17,6 +17,7 @@ extern int g_merge_gates;
 extern int g_group_kernel;
 extern int g_shape_max_bits;
 extern int g_dense_tensor_cores;
+extern int g_fx_tensor;
 extern int g_fx_min_blocks;
 int read_clear_device_error(int* flags, cudaStream_t stream);
 int apply_dense_gate(const void* in, void* out, int n, int layout, int k, const int* bits, const double* mat,
@@ -126,6 +127,12 @@ int qf_set_tile_kernel(int mode) {
 int qf_set_fx_occupancy(int min_blocks) {
   if (min_blocks < 1 || min_blocks > 4) return QF_ERR_INVALID_ARGUMENT;
   g_fx_min_blocks = min_blocks;
+  return QF_OK;
+}
+
+int qf_set_fx_tensor_cores(int on) {
+  if (on < 0 || on > 1) return QF_ERR_INVALID_ARGUMENT;
+  g_fx_tensor = on;
   return QF_OK;
 }
 

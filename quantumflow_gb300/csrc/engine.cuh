@@ -272,6 +272,28 @@ int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int f
                int* passes_out);
 int fx_plan_stats(int n, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks, int* nblocks);
 
+// Tensor-core complex128 passes (tcfx.cu): the unitary U (16 x 16) of a run
+// of gates and window sign ops on four window bits, applied to every row of
+// 16 amplitudes in an integer-digit fixed-point arithmetic on fp16 MMAs.
+// Sign ops with bits outside the window run on the inputs (before every
+// dense gate on their window bits) or on the outputs.
+constexpr int TX_MAX_SIGNS = 48;
+struct TxParams {
+  const void* in;
+  void* out;
+  int* err;
+  int32_t n, nin, nout, pad;
+  int32_t sbits[4];                 // window bits, ascending
+  int64_t off[16];                  // global offset of window index c
+  int64_t g[16][16][2];             // U as round(entry * 2^62): [out c][in c][re, im]
+  uint64_t in_mout[TX_MAX_SIGNS];   // input-side sign ops: their bits outside the window
+  uint64_t out_mout[TX_MAX_SIGNS];  // output-side sign ops
+  uint16_t in_rmask[TX_MAX_SIGNS];  // window indices c that carry all of the op's window bits
+  uint16_t out_rmask[TX_MAX_SIGNS];
+};
+int tx_launch(const TxParams& P, cudaStream_t stream);
+extern int g_fx_tensor;  // qf_set_fx_tensor_cores (1: tensor-core passes where they apply)
+
 int device_sm_count();
 int timing_enable(int on);
 int timing_collect(double* ms, int64_t* counts, int nkinds);

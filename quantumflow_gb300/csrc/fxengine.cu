@@ -24,6 +24,8 @@
 
 namespace qf {
 
+int* device_error_word();
+
 // ------------------------------------------------------------- device ----
 // largest FP64 exponent field among the parts of v[]
 template <int R>
@@ -642,7 +644,7 @@ constexpr int FX_G_MAX = 4;
 // do not take close the pass and run alone in native FP64.
 std::vector<FxBlock> fx_split_shapes(std::vector<FxBlock>& blocks, const std::vector<HostOp>& ops);
 
-std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
+std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k, bool split = true) {
   if (fusion_k <= 0) fusion_k = FX_G_MAX;
   if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
   // generalised permutations on <= 2 qubits with unit-modulus entries run as
@@ -686,7 +688,7 @@ std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k) {
     cur.ncoef += need;
   }
   close();
-  return fx_split_shapes(blocks, ops);
+  return split ? fx_split_shapes(blocks, ops) : blocks;
 }
 
 // Passes made of dense gates and signs only are cut where their next dense
@@ -917,8 +919,9 @@ int fx_group_launch(const FxGroupParams& P, int G, cudaStream_t stream) {
 }
 
 // kernel used by a block: 0 element-wise group pass, 1 direct sweep,
-// 3 group pass, 4 shape pass, 5 native FP64 op
+// 3 group pass, 4 shape pass, 5 native FP64 op, 6 tensor-core pass
 int fx_block_kernel(const std::vector<HostOp>& ops, const FxBlock& B) {
+  if (B.shape == -2) return 6;
   if (B.native) return 5;
   if (B.G == 0) return 0;
   if (B.idx.size() == 1) return 1;
@@ -1022,11 +1025,176 @@ int fx_shape_launch(const FxShapeParams& P, cudaStream_t stream) {
   return check_cuda(cudaGetLastError());
 }
 
+// Fill the tensor-core pass of block B (dense unitary gates, unit-modulus
+// diagonals and phases on its window, sign ops), or return
+// QF_ERR_NOT_SUPPORTED.  The window is the block's dense bits, padded to
+// four with the highest bits outside them (the rows then keep the low
+// bits, so a warp's accesses stay contiguous).  U is multiplied up in long
+// double from the gates in block order; a sign op with bits outside the
+// window is moved to the inputs when no earlier dense gate of the block
+// touches its window bits, else to the outputs when no later one does.
+int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams& P) {
+  if (B.native || B.G < 1 || B.G > 4 || n < 11) return QF_ERR_NOT_SUPPORTED;
+  using lcplx = std::complex<long double>;
+  int wb[4], nw = 0;
+  for (int j = 0; j < B.G; ++j) wb[nw++] = B.order[j];
+  for (int bit = n - 1; nw < 4 && bit >= 0; --bit)
+    if (std::find(wb, wb + nw, bit) == wb + nw) wb[nw++] = bit;
+  auto pos = [&](int bit) {
+    for (int j = 0; j < 4; ++j)
+      if (wb[j] == bit) return j;
+    return -1;
+  };
+  uint64_t wmask = 0;
+  for (int j = 0; j < 4; ++j) wmask |= uint64_t(1) << wb[j];
+  std::memset(&P, 0, sizeof(TxParams));
+  P.n = n;
+  int sb[4] = {wb[0], wb[1], wb[2], wb[3]};
+  std::sort(sb, sb + 4);
+  for (int j = 0; j < 4; ++j) P.sbits[j] = sb[j];
+  for (int c = 0; c < 16; ++c) {
+    int64_t o = 0;
+    for (int j = 0; j < 4; ++j)
+      if ((c >> j) & 1) o |= int64_t(1) << wb[j];
+    P.off[c] = o;
+  }
+  std::vector<lcplx> U(256, lcplx(0, 0)), T(256);
+  for (int c = 0; c < 16; ++c) U[c * 16 + c] = 1;
+  // window bits each dense op of the block touches, for the sign placement
+  std::vector<int> dense_pos;
+  std::vector<uint32_t> dense_bits;
+  for (int k = 0; k < (int)B.idx.size(); ++k) {
+    const HostOp& op = ops[B.idx[k]];
+    if (op.type == OP_DENSE1 || op.type == OP_DENSE2) {
+      uint32_t m = 0;
+      for (int j = 0; j < op.k; ++j) m |= 1u << pos(op.gb[j]);
+      dense_pos.push_back(k);
+      dense_bits.push_back(m);
+    }
+  }
+  for (int k = 0; k < (int)B.idx.size(); ++k) {
+    const HostOp& op = ops[B.idx[k]];
+    if (fx_kind(op) == FXK_NATIVE) return QF_ERR_NOT_SUPPORTED;
+    if (op.type == OP_DENSE1 || op.type == OP_DENSE2) {
+      int jp[2];
+      for (int j = 0; j < op.k; ++j) jp[j] = pos(op.gb[j]);
+      const int D = 1 << op.k;
+      uint32_t om = 0;
+      for (int j = 0; j < op.k; ++j) om |= 1u << jp[j];
+      auto local = [&](int c) {  // the gate's matrix index of window index c (gate qubit 0 = MSB)
+        int r = 0;
+        for (int j = 0; j < op.k; ++j) r = (r << 1) | ((c >> jp[j]) & 1);
+        return r;
+      };
+      // T = E U with E the gate embedded in the window
+      for (int r = 0; r < 16; ++r)
+        for (int c = 0; c < 16; ++c) {
+          lcplx acc(0, 0);
+          const int lr = local(r);
+          for (int m = 0; m < D; ++m) {
+            int cm = r & ~static_cast<int>(om);
+            for (int j = 0; j < op.k; ++j)
+              if ((m >> (op.k - 1 - j)) & 1) cm |= 1 << jp[j];
+            const cplx g = op.m[lr * D + m];
+            acc += lcplx(g.real(), g.imag()) * U[cm * 16 + c];
+          }
+          T[r * 16 + c] = acc;
+        }
+      U.swap(T);
+      continue;
+    }
+    if (op.type == OP_PHASE) {
+      const lcplx s(op.scalar.real(), op.scalar.imag());
+      for (lcplx& v : U) v *= s;
+      continue;
+    }
+    if (op.type == OP_DIAG) {
+      int jp[3];
+      for (int j = 0; j < op.k; ++j) {
+        jp[j] = pos(op.gb[j]);
+        if (jp[j] < 0) return QF_ERR_NOT_SUPPORTED;
+      }
+      for (int r = 0; r < 16; ++r) {
+        int e = 0;
+        for (int j = 0; j < op.k; ++j) e = (e << 1) | ((r >> jp[j]) & 1);
+        const lcplx d(op.diag[e].real(), op.diag[e].imag());
+        for (int c = 0; c < 16; ++c) U[r * 16 + c] *= d;
+      }
+      continue;
+    }
+    if (op.type != OP_SIGN) return QF_ERR_NOT_SUPPORTED;
+    uint32_t jm = 0;
+    uint64_t mo = 0;
+    for (int j = 0; j < op.k; ++j) {
+      const int p = pos(op.gb[j]);
+      if (p >= 0) jm |= 1u << p;
+      else mo |= uint64_t(1) << op.gb[j];
+    }
+    uint32_t rm = 0;
+    for (int c = 0; c < 16; ++c)
+      if ((c & jm) == jm) rm |= 1u << c;
+    if (mo == 0) {  // inside the window: a diagonal of U
+      for (int r = 0; r < 16; ++r)
+        if ((rm >> r) & 1)
+          for (int c = 0; c < 16; ++c) U[r * 16 + c] = -U[r * 16 + c];
+      continue;
+    }
+    bool before = false, after = false;
+    for (size_t d = 0; d < dense_pos.size(); ++d) {
+      if (!(dense_bits[d] & jm)) continue;
+      if (dense_pos[d] < k) before = true;
+      else after = true;
+    }
+    if (!before) {
+      if (P.nin >= TX_MAX_SIGNS) return QF_ERR_NOT_SUPPORTED;
+      P.in_mout[P.nin] = mo;
+      P.in_rmask[P.nin++] = (uint16_t)rm;
+    } else if (!after) {
+      if (P.nout >= TX_MAX_SIGNS) return QF_ERR_NOT_SUPPORTED;
+      P.out_mout[P.nout] = mo;
+      P.out_rmask[P.nout++] = (uint16_t)rm;
+    } else {
+      return QF_ERR_NOT_SUPPORTED;
+    }
+  }
+  (void)wmask;
+  for (int r = 0; r < 16; ++r)
+    for (int c = 0; c < 16; ++c) {
+      const lcplx v = U[r * 16 + c];
+      if (std::abs(v.real()) > 1.0L + 1e-9L || std::abs(v.imag()) > 1.0L + 1e-9L) return QF_ERR_NOT_SUPPORTED;
+      P.g[r][c][0] = std::llround(std::ldexp(v.real(), 62));
+      P.g[r][c][1] = std::llround(std::ldexp(v.imag(), 62));
+    }
+  return QF_OK;
+}
+
 }  // namespace
+
+// The passes to run: blocks the tensor-core pass takes stay whole (shape
+// -2), the others are cut into straight-line shapes as before.
+std::vector<FxBlock> fx_plan_final(std::vector<HostOp>& ops, int n, int& fusion_k) {
+  if (!g_fx_tensor || n < 11) return fx_plan(ops, n, fusion_k);
+  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k, false);
+  std::vector<FxBlock> out;
+  out.reserve(blocks.size());
+  static thread_local TxParams tp;  // ~5 KiB: kept off the stack
+  for (FxBlock& B : blocks) {
+    // a lone 2x2 gate streams faster through the CUDA-core sweep
+    const bool lone2x2 = B.idx.size() == 1 && ops[B.idx[0]].type == OP_DENSE1;
+    if (!lone2x2 && tx_prepare(n, ops, B, tp) == QF_OK) {
+      B.shape = -2;
+      out.push_back(std::move(B));
+      continue;
+    }
+    std::vector<FxBlock> one(1, std::move(B));
+    for (FxBlock& b : fx_split_shapes(one, ops)) out.push_back(std::move(b));
+  }
+  return out;
+}
 
 int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int fusion_k, cudaStream_t stream,
                int* passes_out) {
-  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k);
+  std::vector<FxBlock> blocks = fx_plan_final(ops, n, fusion_k);
   int passes = 0;
   const void* src = in;
   if (blocks.empty()) {
@@ -1041,9 +1209,21 @@ int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int f
   }
   static thread_local FxGroupParams gp;  // ~18 KiB: kept off the stack
   static thread_local FxShapeParams sp;
+  static thread_local TxParams tp;
   for (FxBlock& B : blocks) {
     int rc;
     switch (fx_block_kernel(ops, B)) {
+      case 6: {
+        rc = tx_prepare(n, ops, B, tp);
+        if (rc) return rc;
+        tp.in = src;
+        tp.out = out;
+        tp.err = device_error_word();
+        if (tp.err == nullptr) return QF_ERR_CUDA;
+        LaunchTimer timer(QF_KERNEL_FX_TENSOR, stream);
+        rc = tx_launch(tp, stream);
+        break;
+      }
       case 4: {
         rc = fx_shape_prepare(n, ops, B, sp);
         if (rc) return rc;
@@ -1083,7 +1263,7 @@ int fx_run_ops(const void* in, void* out, int n, std::vector<HostOp>& ops, int f
 }
 
 int fx_plan_stats(int n, std::vector<HostOp>& ops, int fusion_k, int32_t* stats, int max_blocks, int* nblocks) {
-  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k);
+  std::vector<FxBlock> blocks = fx_plan_final(ops, n, fusion_k);
   *nblocks = (int)blocks.size();
   for (int b = 0; b < (int)blocks.size() && b < max_blocks; ++b) {
     const FxBlock& B = blocks[b];

@@ -1,0 +1,552 @@
+// Complex128 gate passes on the 5th-generation tensor cores at FP64-class
+// precision: integer digits of a fixed-point form, multiplied by fp16 MMAs
+// (tcgen05.mma kind::f16) whose FP32 accumulators stay exact.
+//
+// Reference semantics: quantumflow/backend/numpybk.py:159-214 tensormul
+// applied gate by gate (quantumflow/circuits.py:87-99).  A pass applies a
+// run of unitary gates whose dense qubits lie in a window of four bits,
+// with CZ-like sign ops around them: the host multiplies them into one
+// 16x16 unitary U (long double) and the pass computes y = U x for every
+// "row" x, the 16 amplitudes that differ only in the window bits.
+//
+// Arithmetic (an integer form of the Ozaki splitting scheme: Ozaki, Ogita,
+// Oishi and Rump, "Error-free transformations of matrix multiplication by
+// using fast routines of matrix multiplication", Numer. Algorithms 59, 2012):
+//
+//  * a row's 32 real parts share one exponent E (the largest FP64 exponent
+//    field among them); each part becomes A = v * 2^(1022 + 61 - E)
+//    truncated toward zero, |A| < 2^61, with integer bit operations (the
+//    FP64 pipe is the narrowest unit on this part);
+//  * U's real form (32 x 32) is G = round(g * 2^62), |G| <= 2^62;
+//  * both are written in base 256 with balanced digits: X + 0x8080..80 =
+//    sum_t (d_t + 128) 256^(7-t), d_t in [-128, 127], so a byte of the
+//    biased integer is a digit (one byte permute per digit pair) and every
+//    digit is exact in fp16;
+//  * A.G = sum_delta acc_delta 256^(14 - delta), acc_delta = sum over the
+//    digit pairs t + u = delta of the digit GEMMs; delta = 0..7 are kept
+//    (36 of the 64 digit products).  With K = 32 terms per output every
+//    acc_delta is an integer below 2^22 (the top digits are small:
+//    |d_0(A)| <= 33, |d_0(G)| <= 65; the largest, acc_7, is at most
+//    32 (33 128 + 6 128^2 + 128 65) < 2^21.8), so the FP32 accumulation is
+//    exact and so is a float-to-integer conversion by the 1.5 * 2^23
+//    addition trick;
+//  * Z = A.G / 2^63 = sum acc_delta 2^(49 - 8 delta) (two's complement
+//    int64; |Z| <= 2^62.5 because U is unitary), converted to FP64 once,
+//    exactly rounded, and scaled by 2^(E - 1082).
+//
+// Error per output, relative to the row's largest part: the truncation of
+// the inputs (each below 2^-59 of it; through a unit row of U at most
+// sqrt(32) 2^-59 = 2^-56.5), the dropped digit products (delta >= 8: a few
+// 2^-63 typically) and one FP64 rounding of the output -- below the error of
+// FP64 arithmetic on the same row.  The CPU model of this arithmetic
+// (tests/txarith.py) measures it against exact rational arithmetic.
+//
+// Kernel: one CTA of 512 threads per SM, persistent over tiles of 128 rows
+// (the MMA's M), two stages.  Warps 0-7 convert: two threads per row (lanes
+// l and l ^ 8, eight amplitudes each; the row exponent is a shuffle away)
+// turn their amplitudes into digits and store them as the A operand, K-major
+// rows of 8 digits x 32 reals in four 128-byte swizzled chunks.  The gate's
+// digits (B: 8 digit blocks x 32 output reals, K = 32 input reals) are built
+// once per CTA.  Thread 0 issues, per amplitude digit t, two MMAs (K = 16
+// each) against the first 32 (8 - t) rows of B into tensor-memory columns
+// [32 t, 256) of the stage: column block delta receives every digit product
+// of its weight.  Warps 8-15 run the epilogue: the thread of TMEM lane r
+// (two per row, 16 output reals each) reads the eight accumulators of each
+// output, combines them into Z and stores FP64.  Conversion, MMAs and
+// epilogue of consecutive tiles overlap.  Every wait is bounded (4 s): on
+// expiry the kernel raises the device error word and every thread leaves
+// its loop.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <cuda_fp16.h>
+
+#include "engine.cuh"
+#include "fx.cuh"
+
+namespace qf {
+
+int* device_error_word();
+int g_fx_tensor = 1;  // qf_set_fx_tensor_cores
+
+namespace {
+
+constexpr int TX_ROWS = 128;     // rows per tile (MMA M)
+constexpr int TX_KD = 32;        // real width of a row (GEMM K) and of U (GEMM N per digit)
+constexpr int TX_ND = 8;         // base-256 digits per integer
+constexpr int TX_MB = 61;        // amplitude integers: |A| < 2^61
+constexpr uint64_t TX_BIAS = 0x8080808080808080ull;
+constexpr uint32_t TX_A_CHUNK = TX_ROWS * 128;         // 64 fp16 of K per row, 128-byte rows
+constexpr uint32_t TX_A_BYTES = 4 * TX_A_CHUNK;        // 8 digits x 32 reals = 256 K per row
+constexpr uint32_t TX_B_BYTES = TX_ND * TX_KD * 128;   // 256 N-rows, 32 K used of each 128-byte row
+constexpr float TX_MAGIC = 12582912.0f;  // 1.5 * 2^23
+constexpr int32_t TX_MAGIC_BITS = 0x4B400000;
+
+QF_D uint32_t tx_smem(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+// canonical K-major, 128-byte swizzled shared-memory matrix descriptor
+QF_D uint64_t tx_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= static_cast<uint64_t>(1) << 16;                   // leading byte offset (unused when swizzled)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
+  d |= static_cast<uint64_t>(1) << 46;                   // descriptor version
+  d |= static_cast<uint64_t>(2) << 61;                   // 128-byte swizzle
+  return d;
+}
+// instruction descriptor: D f32, A and B f16, both K-major, M = 128
+QF_D uint32_t tx_idesc(int N) {
+  return (1u << 4) | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(TX_ROWS >> 4) << 24);
+}
+// byte offset of the 16-byte piece p (0..7) of row r in a 128-byte swizzled chunk
+QF_D uint32_t tx_piece(int r, int p) { return static_cast<uint32_t>(r * 128 + ((p ^ (r & 7)) << 4)); }
+
+QF_D void tx_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+QF_D void tx_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tx_smem(bar))
+               : "memory");
+}
+QF_D void tx_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+QF_D void tx_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// waits for the phase to complete, suspended up to about 100 us per try
+QF_D bool tx_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(tx_smem(bar)), "r"(parity), "r"(100000u)
+      : "memory");
+  return ok != 0;
+}
+QF_D uint64_t tx_now() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+// bounded wait (4 s of wall clock); false (and the error word raised) on expiry
+QF_D bool tx_wait(uint64_t* bar, uint32_t parity, int* err) {
+  if (tx_try_wait(bar, parity)) return true;
+  const uint64_t t0 = tx_now();
+  while (!tx_try_wait(bar, parity)) {
+    if (tx_now() - t0 > 4000000000ull) {
+      atomicOr(err, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
+// 4 consecutive fp32 accumulator columns of this warp's 32 TMEM lanes
+// (the caller waits with tx_wait_ld before reading)
+QF_D void tx_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
+// wait for this thread's tensor-memory loads; the registers pass through the
+// asm so that no use of them is scheduled before the wait
+QF_D void tx_wait_ld(uint32_t (&a)[8][4]) {
+  asm volatile(
+      "tcgen05.wait::ld.sync.aligned;"
+      : "+r"(a[0][0]), "+r"(a[0][1]), "+r"(a[0][2]), "+r"(a[0][3]), "+r"(a[1][0]), "+r"(a[1][1]), "+r"(a[1][2]),
+        "+r"(a[1][3]), "+r"(a[2][0]), "+r"(a[2][1]), "+r"(a[2][2]), "+r"(a[2][3]), "+r"(a[3][0]), "+r"(a[3][1]),
+        "+r"(a[3][2]), "+r"(a[3][3]), "+r"(a[4][0]), "+r"(a[4][1]), "+r"(a[4][2]), "+r"(a[4][3]), "+r"(a[5][0]),
+        "+r"(a[5][1]), "+r"(a[5][2]), "+r"(a[5][3]), "+r"(a[6][0]), "+r"(a[6][1]), "+r"(a[6][2]), "+r"(a[6][3]),
+        "+r"(a[7][0]), "+r"(a[7][1]), "+r"(a[7][2]), "+r"(a[7][3])
+      :
+      : "memory");
+}
+
+// Biased fixed-point integer of one part: A + TX_BIAS, A = v * 2^(1022 +
+// 61 - E) truncated toward zero (Ep = E + 3 >= the part's exponent field +
+// 3).  The 64-bit mantissa with its hidden bit at bit 63 is shifted right by
+// n = Ep - e with clamped funnel shifts (no selects); zeros and subnormals
+// (n >= 67) shift out completely.  The sign and the bias are one add:
+// (t ^ neg) - neg + BIAS = (t ^ neg) + BIAS + (neg & 1).
+QF_D uint64_t tx_biased(double v, uint32_t Ep) {
+  const uint32_t hi = fx_hiword(v), lo = fx_loword(v);
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  const uint32_t mh = __funnelshift_l(lo, hi, 11) | 0x80000000u;
+  const uint32_t ml = lo << 11;
+  const uint32_t n = Ep - e;
+  uint32_t tl = __funnelshift_rc(ml, mh, n);             // low word of m >> min(n, 32)
+  const uint32_t th = __funnelshift_rc(mh, 0u, n);        // high word (0 once n >= 32)
+  tl = __funnelshift_rc(tl, 0u, n > 32u ? n - 32u : 0u);  // the rest of a shift past 32 (0 past 64)
+  const uint32_t neg = static_cast<uint32_t>(static_cast<int32_t>(hi) >> 31);
+  const uint64_t t = (static_cast<uint64_t>(th ^ neg) << 32) | (tl ^ neg);
+  return t + TX_BIAS + (neg & 1u);
+}
+
+// fp16x2 word of digit t (0 = most significant) of two biased integers:
+// low half from x, high half from y; each half is the fp16 number
+// byte - 128 (byte | 0x6400 is the fp16 value 1024 + byte).
+template <int T>
+QF_D uint32_t tx_digit_pair(uint64_t x, uint64_t y) {
+  constexpr int byte = 7 - T;  // little-endian byte index within the 64-bit integer
+  const uint32_t xw = byte >= 4 ? static_cast<uint32_t>(x >> 32) : static_cast<uint32_t>(x);
+  const uint32_t yw = byte >= 4 ? static_cast<uint32_t>(y >> 32) : static_cast<uint32_t>(y);
+  constexpr uint32_t b = byte & 3;
+  // selector: byte b of xw into byte 0, byte b of yw (source bytes 4..7) into byte 2
+  // selector nibbles: result byte 0 <- byte b of xw, result byte 2 <- byte b of yw
+  const uint32_t w = __byte_perm(xw, yw, b | ((4u + b) << 8)) & 0x00FF00FFu;
+  const uint32_t biased = w | 0x64006400u;
+  __half2 r = *reinterpret_cast<const __half2*>(&biased);
+  r = __hsub2(r, __halves2half2(__float2half_rn(1152.f), __float2half_rn(1152.f)));
+  return *reinterpret_cast<uint32_t*>(&r);
+}
+
+// Z = sum_delta acc_delta 2^(49 - 8 delta) (= A.G / 2^63) from the eight
+// accumulator words (FP32 integers below 2^22): each becomes 1.5 * 2^23 +
+// acc exactly, whose bit pattern is TX_MAGIC_BITS + acc; pairs are joined in
+// int32 (acc_2j 2^8 + acc_2j+1 < 2^31) and the biases cancel in one
+// constant.  The shifts and adds are multiply-adds (the FMA pipe), the
+// integer ALU being the busiest unit of this kernel.
+QF_D int64_t tx_combine(const uint32_t (&w)[8]) {
+  uint32_t b[8];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) b[d] = __float_as_uint(__uint_as_float(w[d]) + TX_MAGIC);
+  constexpr uint32_t K2 = static_cast<uint32_t>(TX_MAGIC_BITS) * 257u;  // bias of one joined pair (mod 2^32)
+  const int32_t p0 = static_cast<int32_t>(b[0] * 256u + b[1] - K2);
+  const int32_t p1 = static_cast<int32_t>(b[2] * 256u + b[3] - K2);
+  const int32_t p2 = static_cast<int32_t>(b[4] * 256u + b[5] - K2);
+  const int32_t p3 = static_cast<int32_t>(b[6] * 256u + b[7] - K2);
+  // two's complement sums wrap mod 2^64; the true Z fits int64
+  int64_t z = fx_mad(p2, 1 << 9, static_cast<int64_t>(p3 >> 7));
+  z = fx_mad(p1, 1 << 25, z);
+  const uint32_t zh = static_cast<uint32_t>(static_cast<uint64_t>(z) >> 32) + static_cast<uint32_t>(p0) * 512u;
+  return static_cast<int64_t>((static_cast<uint64_t>(zh) << 32) | static_cast<uint32_t>(z));
+}
+
+// FP64 value of Z * 2^(E - 1082), its sign flipped when sg is the sign
+// bit: Z is converted exactly rounded by the FP64 pipe's convert, and the
+// power of two (delta = (E - 1082) << 20) and the sign flip (adding 2^31
+// mod 2^32) are one add on the high word.  E >= 64 and |Z| >= 1 keep the
+// result normal; Z = 0 gives 0.
+QF_D double tx_out(int64_t Z, uint32_t delta, uint32_t sg) {
+  const double d = __ll2double_rn(Z);
+  const uint32_t hi = fx_hiword(d);
+  return fx_double(hi != 0u ? hi + delta + sg : 0u, fx_loword(d));
+}
+
+// ------------------------------------------------------------ pass parts ----
+// B: row 32 u + o (digit u of output real o = 2 r + p), K = input real
+// 2 c + q; one fp16x2 word (q = 0, 1) per (u, r, c, p)
+QF_D void tx_build_b(const TxParams& P, unsigned char* sb, int tid, int nthreads) {
+  for (int w = tid; w < TX_ND * 16 * 16 * 2; w += nthreads) {
+    const int p = w & 1, c = (w >> 1) & 15, r = (w >> 5) & 15, u = w >> 9;
+    const int64_t gre = P.g[r][c][0], gim = P.g[r][c][1];
+    // real form: re out = (Re, -Im) . (re, im); im out = (Im, Re) . (re, im)
+    const uint64_t x = static_cast<uint64_t>(p == 0 ? gre : gim) + TX_BIAS;
+    const uint64_t y = static_cast<uint64_t>(p == 0 ? -gim : gre) + TX_BIAS;
+    uint32_t word;
+    switch (u) {
+      case 0: word = tx_digit_pair<0>(x, y); break;
+      case 1: word = tx_digit_pair<1>(x, y); break;
+      case 2: word = tx_digit_pair<2>(x, y); break;
+      case 3: word = tx_digit_pair<3>(x, y); break;
+      case 4: word = tx_digit_pair<4>(x, y); break;
+      case 5: word = tx_digit_pair<5>(x, y); break;
+      case 6: word = tx_digit_pair<6>(x, y); break;
+      default: word = tx_digit_pair<7>(x, y); break;
+    }
+    const int row = 32 * u + 2 * r + p, k = 2 * c;  // fp16 element k, k + 1 of the row
+    *reinterpret_cast<uint32_t*>(sb + tx_piece(row, k >> 3) + (k & 7) * 2) = word;
+  }
+}
+
+// Global index of a row with its window bits zero: the row index's bits
+// are spread over the non-window bits.  The tile part (tile * 128, the same
+// for every thread) and the row-in-tile part map independently.
+QF_D int64_t tx_spread(const TxParams& P, int64_t x) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) x = insert0(x, P.sbits[j]);
+  return x;
+}
+
+// the amplitudes j0 .. j0 + 3 of a thread's half-row (base b: the row's
+// base with the half's window bit already set)
+QF_D void tx_load_half(const TxParams& P, const double2* __restrict__ in, double2 (&x)[8], int j0, int64_t b) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) x[j0 + j] = in[b | P.off[j0 + j]];
+}
+
+// Row exponent of a thread's half-row and its partner's (lane ^ 8): the
+// largest FP64 exponent field (4095 for rows below 2^-959, which become 0).
+QF_D int tx_rowexp(const double2 (&x)[8]) {
+  uint32_t mx = 0u;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    mx = max(mx, fx_hiword(x[j].x) & 0x7fffffffu);
+    mx = max(mx, fx_hiword(x[j].y) & 0x7fffffffu);
+  }
+  mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+  return static_cast<int>(mx >> 20) < FX_EMIN ? 4095 : static_cast<int>(mx >> 20);
+}
+
+// Input half-row of one thread: its 8 amplitudes (window indices 8 ih + j)
+// of row irow, after the input-side signs, become digits in A (sa), scaled
+// by the row exponent E (tx_rowexp), which goes to rowE[irow].  b is the
+// half-row's base (the input-side signs test it).
+QF_D void tx_convert(const TxParams& P, double2 (&x)[8], unsigned char* sa, int* rowE, int64_t b, int irow, int ih,
+                     int E) {
+  if (P.nin > 0) {
+    uint32_t fl = 0u;
+    for (int s = 0; s < P.nin; ++s)
+      if ((static_cast<uint64_t>(b) & P.in_mout[s]) == P.in_mout[s]) fl ^= P.in_rmask[s];
+    fl = (fl >> (8 * ih)) & 0xFFu;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint32_t sg = ((fl >> j) & 1u) << 31;
+      x[j] = make_double2(fx_double(fx_hiword(x[j].x) ^ sg, fx_loword(x[j].x)),
+                          fx_double(fx_hiword(x[j].y) ^ sg, fx_loword(x[j].y)));
+    }
+  }
+  if (ih == 0) rowE[irow] = E;
+  const uint32_t Ep = static_cast<uint32_t>(E + 64 - TX_MB);
+#pragma unroll
+  for (int j0 = 0; j0 < 8; j0 += 4) {
+    uint64_t ur[4], ui[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      ur[j] = tx_biased(x[j0 + j].x, Ep);
+      ui[j] = tx_biased(x[j0 + j].y, Ep);
+    }
+    // digit t of amplitudes c = 8 ih + j0 .. + 3: fp16 elements (t & 1) 32 + 2c
+    // of chunk t >> 1, one 16-byte piece
+#define QF_TX_STORE(T)                                                                                   \
+  {                                                                                                      \
+    uint4 v;                                                                                             \
+    v.x = tx_digit_pair<T>(ur[0], ui[0]);                                                               \
+    v.y = tx_digit_pair<T>(ur[1], ui[1]);                                                               \
+    v.z = tx_digit_pair<T>(ur[2], ui[2]);                                                               \
+    v.w = tx_digit_pair<T>(ur[3], ui[3]);                                                               \
+    const int piece = ((T & 1) * 32 + 2 * (8 * ih + j0)) >> 3;                                          \
+    *reinterpret_cast<uint4*>(sa + (T >> 1) * TX_A_CHUNK + tx_piece(irow, piece)) = v;                  \
+  }
+    QF_TX_STORE(0)
+    QF_TX_STORE(1)
+    QF_TX_STORE(2)
+    QF_TX_STORE(3)
+    QF_TX_STORE(4)
+    QF_TX_STORE(5)
+    QF_TX_STORE(6)
+    QF_TX_STORE(7)
+#undef QF_TX_STORE
+  }
+}
+
+// The MMAs of one tile: amplitude digit t against gate digits 0 .. 7 - t,
+// into accumulator columns [acc + 32 t, acc + 256)
+QF_D void tx_issue(uint32_t abase, uint32_t bbase, uint32_t acc) {
+#pragma unroll
+  for (int t = 0; t < TX_ND; ++t) {
+    const uint32_t idesc = tx_idesc(TX_KD * (TX_ND - t));
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+      const uint32_t a = abase + (t >> 1) * TX_A_CHUNK + (t & 1) * 64 + ks * 32;
+      const uint32_t b = bbase + ks * 32;
+      tx_mma(acc + static_cast<uint32_t>(TX_KD * t), tx_desc(a), tx_desc(b), idesc, (t > 0 || ks > 0) ? 1u : 0u);
+    }
+  }
+}
+
+// Epilogue of one thread: 16 output reals (amplitudes c = 8 oh + j) of its
+// row (half-row base b) from the accumulators at tensor-memory address acc
+// (lane field set), with the output-side signs, stored as FP64.  The tensor-memory loads of
+// the next four reals are in flight while four are converted.
+QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int64_t b, int oh) {
+  const uint32_t delta = static_cast<uint32_t>(E - 1082) << 20;
+  uint32_t fl = 0u;
+  for (int s = 0; s < P.nout; ++s)
+    if ((static_cast<uint64_t>(b) & P.out_mout[s]) == P.out_mout[s]) fl ^= P.out_rmask[s];
+  fl = (fl >> (8 * oh)) & 0xFFu;
+  uint32_t a4[2][8][4];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh), a4[0][d]);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    tx_wait_ld(a4[q & 1]);
+    if (q < 3) {
+#pragma unroll
+      for (int d = 0; d < 8; ++d)
+        tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh + 4 * (q + 1)), a4[(q + 1) & 1][d]);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const int j = 2 * q + a;
+      uint32_t wr[8], wi[8];
+#pragma unroll
+      for (int d = 0; d < 8; ++d) {
+        wr[d] = a4[q & 1][d][2 * a];
+        wi[d] = a4[q & 1][d][2 * a + 1];
+      }
+      const uint32_t sg = ((fl >> j) & 1u) << 31;
+      out[b | P.off[j]] = make_double2(tx_out(tx_combine(wr), delta, sg), tx_out(tx_combine(wi), delta, sg));
+    }
+  }
+}
+
+QF_D void tx_alloc(uint32_t* slot, uint32_t cols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tx_smem(slot)), "r"(cols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+QF_D void tx_bar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tx_smem(bar)), "r"(count) : "memory");
+}
+QF_D void tx_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tx_smem(bar)) : "memory");
+}
+// barrier `id` over `count` threads, returning whether any of them passed v != 0
+QF_D int tx_bar_or(int id, int count, int v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\t"
+      "barrier.cta.red.or.pred q, %2, %3, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(v), "r"(id), "r"(count)
+      : "memory");
+  return r;
+}
+
+// ------------------------------------------------ warp-specialised kernel ----
+// One CTA of 512 threads per SM, two stages of A, rowE and accumulators.
+// Warps 0-7 convert tile i into stage i & 1 (after the epilogue of tile
+// i - 2 released it), meet at a named barrier, and thread 0 marks the
+// stage's row exponents written (conv_done) and issues the tile's MMAs,
+// committed to mma_done[stage].  Warps 8-15 wait for both, run the
+// epilogue from the stage's accumulators and release the stage (tmem_free,
+// one arrival per warp).  Conversion of one tile, the MMAs of
+// the next and the epilogue of the one before run at the same time.
+constexpr int TP_THREADS = 512;
+constexpr uint32_t TP_SMEM = 2 * TX_A_BYTES + TX_B_BYTES + 1024;
+constexpr int TP_TMEM_COLS = 512;
+
+__global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant__ TxParams P) {
+  extern __shared__ __align__(1024) unsigned char tx_raw[];
+  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tx_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* sb = sm + 2 * TX_A_BYTES;
+  __shared__ __align__(8) uint64_t mma_done[2], conv_done[2], tmem_free[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int rowE[2][TX_ROWS];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  tx_build_b(P, sb, tid, TP_THREADS);
+  if (warp == 0) tx_alloc(&tmem_slot, TP_TMEM_COLS);
+  if (tid == 0) {
+    tx_bar_init(&mma_done[0], 1);
+    tx_bar_init(&mma_done[1], 1);
+    tx_bar_init(&conv_done[0], 1);
+    tx_bar_init(&conv_done[1], 1);
+    tx_bar_init(&tmem_free[0], 8);
+    tx_bar_init(&tmem_free[1], 8);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tx_fence_before();
+  __syncthreads();
+  tx_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
+  if (warp < 8) {
+    // ---- converters and the MMA issuer.  The loads of tile i + 1 are
+    // issued before tile i is converted, into a second register set, so a
+    // whole iteration hides their latency.
+    const double2* __restrict__ in = static_cast<const double2*>(P.in);
+    const uint32_t bbase = tx_smem(sb);
+    const int irow = warp * 16 + (lane & 7) + ((lane >> 4) << 3), ih = (lane >> 3) & 1;
+    const int64_t hrow = tx_spread(P, irow) | (ih ? P.off[8] : 0);  // this half-row within its tile
+    const int64_t step = gridDim.x;
+    double2 x[8], xn[8];
+    int64_t tile = blockIdx.x;
+    if (tile < ntiles) {
+      const int64_t b = tx_spread(P, tile * TX_ROWS) | hrow;
+      tx_load_half(P, in, x, 0, b);
+      tx_load_half(P, in, x, 4, b);
+    }
+    int fail = 0;
+    for (int it = 0; tile < ntiles; tile += step, ++it) {
+      const int s = it & 1;
+      const bool more = tile + step < ntiles;
+      if (more) {
+        const int64_t nb = tx_spread(P, (tile + step) * TX_ROWS) | hrow;
+        tx_load_half(P, in, xn, 0, nb);
+        tx_load_half(P, in, xn, 4, nb);
+      }
+      bool ok = true;
+      if (it >= 2) ok = tx_wait(&tmem_free[s], static_cast<uint32_t>((it >> 1) - 1) & 1u, P.err);
+      if (!__all_sync(0xffffffffu, ok)) fail = 1;  // warp-uniform: the row exponent shuffles within the warp
+      tx_fence_after();
+      unsigned char* sa = sm + s * TX_A_BYTES;
+      if (!fail) tx_convert(P, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | hrow, irow, ih, tx_rowexp(x));
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (tx_bar_or(1, 256, fail)) break;
+      if (tid == 0) {
+        tx_arrive(&conv_done[s]);  // the row exponents of this stage are written
+        tx_fence_after();
+        tx_issue(tx_smem(sa), bbase, tmem + static_cast<uint32_t>(256 * s));
+        tx_commit(&mma_done[s]);
+      }
+      if (more) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = xn[j];
+      }
+    }
+  } else {
+    // ---- epilogue
+    double2* out = static_cast<double2*>(P.out);
+    const int ew = warp - 8;
+    const int orow = 32 * (ew & 3) + lane, oh = ew >> 2;
+    const int64_t hrow = tx_spread(P, orow) | (oh ? P.off[8] : 0);
+    const uint32_t lane_addr = static_cast<uint32_t>(32 * (ew & 3)) << 16;
+    int64_t tile = blockIdx.x;
+    for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it & 1;
+      const uint32_t par = static_cast<uint32_t>(it >> 1) & 1u;
+      const bool ok = tx_wait(&conv_done[s], par, P.err) && tx_wait(&mma_done[s], par, P.err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      tx_fence_after();
+      tx_epilogue(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * s), rowE[s][orow],
+                  tx_spread(P, tile * TX_ROWS) | hrow, oh);
+      tx_fence_before();
+      __syncwarp();
+      if (lane == 0) tx_arrive(&tmem_free[s]);
+    }
+  }
+  tx_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP_TMEM_COLS) : "memory");
+}
+
+}  // namespace
+
+// Launch one tensor-core pass (P.in/out/err set by the caller); the state
+// must have at least 2^11 amplitudes.  Every row is read completely before
+// its outputs are written, by the same CTA, so the pass may run in place.
+int tx_launch(const TxParams& P, cudaStream_t stream) {
+  if (P.n < 11) return QF_ERR_NOT_SUPPORTED;
+  static std::atomic<int> attr_set[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!attr_set[dev].load()) {
+    int rc = check_cuda(cudaFuncSetAttribute(k_txpipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TP_SMEM));
+    if (rc) return rc;
+    attr_set[dev].store(1);
+  }
+  const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
+  int64_t grid = device_sm_count();
+  if (grid > ntiles) grid = ntiles;
+  k_txpipe<<<(int)grid, TP_THREADS, TP_SMEM, stream>>>(P);
+  return check_cuda(cudaGetLastError());
+}
+
+}  // namespace qf

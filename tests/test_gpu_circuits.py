@@ -272,19 +272,20 @@ def test_shape_passes_random_programs(merge, monkeypatch):
     assert seen_shapes >= 10
 
 
-@pytest.mark.parametrize("c128", ["ff", "fx"])
+@pytest.mark.parametrize("c128", ["ff", "fx", "fx_cuda_cores"])
 def test_index_paths_above_2_31_amplitudes(c128, monkeypatch):
     """States of more than 2^31 amplitudes take the 64-bit-index forms of the
-    4x4 sweep and the shape kernels (float-float) or of the fixed-point
-    group and sweep kernels: N=32 complex128 (64 GB per state, 128 GB at the
-    peak), two merged random layers and their inverse must return |0...0> --
-    norm and single-qubit marginals by device reductions, no host copy of
-    the state."""
+    4x4 sweep and the shape kernels (float-float), of the tensor-core passes
+    (fixed point, the default) or of the fixed-point shape kernels (tensor
+    cores off): N=32 complex128 (64 GB per state, 128 GB at the peak), two
+    merged random layers and their inverse must return |0...0> -- norm and
+    single-qubit marginals by device reductions, no host copy of the
+    state."""
     import ctypes
     import quantumflow_gb300 as qf
     from quantumflow_gb300 import _native as nat
     from quantumflow_gb300.states import _reduce
-    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", c128)
+    monkeypatch.setattr(qf.config, "C128_ARITHMETIC", "ff" if c128 == "ff" else "fx")
     layout = nat.LAYOUT_FF if c128 == "ff" else nat.LAYOUT_FX
     N = 32
     free, _ = torch.cuda.mem_get_info()
@@ -303,21 +304,27 @@ def test_index_paths_above_2_31_amplitudes(c128, monkeypatch):
     op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
     stats = np.zeros(8 * 512, np.int32)
     nb = ctypes.c_int()
-    assert nat.lib.qf_plan_circuit(N, layout, nops, op_k.ctypes.data, op_axes.ctypes.data,
-                                   op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
-    kinds = set(stats[:8 * nb.value].reshape(-1, 8)[:, 7])
-    # lone sweeps and shape passes (float-float) / shape passes (fixed point)
-    assert ({1, 4} if c128 == "ff" else {4}) <= kinds
-    ket = circ.run(qf.zero_state(N))
-    assert abs(ket.norm() - 1) < 1e-11
-    back = circ.H.run(ket)
-    del ket
-    assert abs(back.norm() - 1) < 1e-11
-    for axis in (0, 7, 26, 31):
-        p0, p1 = _reduce("qf_qubit_probabilities", back.buffer, nout=2, extra=(axis,))
-        assert abs(p0 - 1) < 1e-11 and abs(p1) < 1e-11
-    del back
-    torch.cuda.empty_cache()
+    if c128 == "fx_cuda_cores":
+        nat.call("qf_set_fx_tensor_cores", 0)
+    try:
+        assert nat.lib.qf_plan_circuit(N, layout, nops, op_k.ctypes.data, op_axes.ctypes.data,
+                                       op_mats.ctypes.data, 0, stats.ctypes.data, 512, ctypes.byref(nb)) == 0
+        kinds = set(stats[:8 * nb.value].reshape(-1, 8)[:, 7])
+        # lone sweeps and shape passes (float-float) / tensor-core passes /
+        # fixed-point shape passes
+        assert {"ff": {1, 4}, "fx": {6}, "fx_cuda_cores": {4}}[c128] <= kinds
+        ket = circ.run(qf.zero_state(N))
+        assert abs(ket.norm() - 1) < 1e-11
+        back = circ.H.run(ket)
+        del ket
+        assert abs(back.norm() - 1) < 1e-11
+        for axis in (0, 7, 26, 31):
+            p0, p1 = _reduce("qf_qubit_probabilities", back.buffer, nout=2, extra=(axis,))
+            assert abs(p0 - 1) < 1e-11 and abs(p1) < 1e-11
+        del back
+    finally:
+        nat.call("qf_set_fx_tensor_cores", 1)
+        torch.cuda.empty_cache()
 
 
 def test_gops_benchmark_tool():
