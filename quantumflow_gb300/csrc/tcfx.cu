@@ -76,6 +76,10 @@ constexpr int TX_KD = 32;        // real width of a row (GEMM K) and of U (GEMM 
 constexpr int TX_ND = 8;         // base-256 digits per integer
 constexpr int TX_MB = 61;        // amplitude integers: |A| < 2^61
 constexpr uint64_t TX_BIAS = 0x8080808080808080ull;
+// the amplitudes' bias: the top byte of A + bias stays below 0x80 (|A| <
+// 2^61 moves it by at most 32), so a sign-replicating byte permute of it
+// gives a zero byte; the digits are the same as with TX_BIAS
+constexpr uint64_t TX_BIAS_A = 0x4080808080808080ull;
 constexpr uint32_t TX_A_CHUNK = TX_ROWS * 128;         // 64 fp16 of K per row, 128-byte rows
 constexpr uint32_t TX_A_BYTES = 4 * TX_A_CHUNK;        // 8 digits x 32 reals = 256 K per row
 constexpr uint32_t TX_B_BYTES = TX_ND * TX_KD * 128;   // 256 N-rows, 32 K used of each 128-byte row
@@ -166,7 +170,7 @@ QF_D void tx_wait_ld(uint32_t (&a)[8][4]) {
       : "memory");
 }
 
-// Biased fixed-point integer of one part: A + TX_BIAS, A = v * 2^(1022 +
+// Biased fixed-point integer of one part: A + TX_BIAS_A, A = v * 2^(1022 +
 // 61 - E) truncated toward zero (Ep = E + 3 >= the part's exponent field +
 // 3).  The 64-bit mantissa with its hidden bit at bit 63 is shifted right by
 // n = Ep - e with clamped funnel shifts (no selects); zeros and subnormals
@@ -183,7 +187,7 @@ QF_D uint64_t tx_biased(double v, uint32_t Ep) {
   tl = __funnelshift_rc(tl, 0u, n > 32u ? n - 32u : 0u);  // the rest of a shift past 32 (0 past 64)
   const uint32_t neg = static_cast<uint32_t>(static_cast<int32_t>(hi) >> 31);
   const uint64_t t = (static_cast<uint64_t>(th ^ neg) << 32) | (tl ^ neg);
-  return t + TX_BIAS + (neg & 1u);
+  return t + TX_BIAS_A + (neg & 1u);
 }
 
 // fp16x2 word of digit t (0 = most significant) of two biased integers:
@@ -202,6 +206,32 @@ QF_D uint32_t tx_digit_pair(uint64_t x, uint64_t y) {
   __half2 r = *reinterpret_cast<const __half2*>(&biased);
   r = __hsub2(r, __halves2half2(__float2half_rn(1152.f), __float2half_rn(1152.f)));
   return *reinterpret_cast<uint32_t*>(&r);
+}
+
+// The same fp16x2 digit word for the amplitudes (biased by TX_BIAS_A).
+// Digits 0-3 (the high words): one byte permute puts the digit bytes in
+// the low byte of each half and zeros above them (sign copies of the top
+// byte), i.e. the fp16 subnormals byte * 2^-24; two exact half-precision
+// multiply-adds make them byte - bias, leaving the integer ALU (the
+// busiest unit) one instruction per word.  Digits 4-7 as tx_digit_pair.
+template <int T>
+QF_D uint32_t tx_digit_pair_a(uint64_t x, uint64_t y) {
+  if constexpr (T >= 4) {
+    return tx_digit_pair<T>(x, y);
+  } else {
+    constexpr uint32_t b = 3 - T;  // byte of the high word
+    const uint32_t xw = static_cast<uint32_t>(x >> 32), yw = static_cast<uint32_t>(y >> 32);
+    // result bytes: byte b of xw, sign of byte 3 of xw, byte b of yw, sign of byte 3 of yw
+    // (prmt's sign-replicating selectors: the __byte_perm intrinsic takes
+    // only the byte index bits of each selector)
+    uint32_t w;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(w) : "r"(xw), "r"(yw), "r"(b | (0xBu << 4) | ((4u + b) << 8) | (0xFu << 12)));
+    constexpr float bias = T == 0 ? 64.f : 128.f;
+    __half2 h = *reinterpret_cast<const __half2*>(&w);
+    const __half2 k = __float2half2_rn(4096.f);
+    h = __hfma2(__hmul2(h, k), k, __float2half2_rn(-bias));
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
 }
 
 // Z = sum_delta acc_delta 2^(49 - 8 delta) (= A.G / 2^63) from the eight
@@ -295,9 +325,12 @@ QF_D int tx_rowexp(const double2 (&x)[8]) {
 // Input half-row of one thread: its 8 amplitudes (window indices 8 ih + j)
 // of row irow, after the input-side signs, become digits in A (sa), scaled
 // by the row exponent E (tx_rowexp), which goes to rowE[irow].  b is the
-// half-row's base (the input-side signs test it).
-QF_D void tx_convert(const TxParams& P, double2 (&x)[8], unsigned char* sa, int* rowE, int64_t b, int irow, int ih,
-                     int E) {
+// half-row's base (the input-side signs test it).  As soon as a group of
+// four amplitudes has become integers, its registers take the loads of the
+// same amplitudes of the next tile (half-row base nb; none when nb < 0), so
+// those are in flight during the rest of this conversion and the MMAs.
+QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 (&x)[8], unsigned char* sa,
+                     int* rowE, int64_t b, int irow, int ih, int E, int64_t nb) {
   if (P.nin > 0) {
     uint32_t fl = 0u;
     for (int s = 0; s < P.nin; ++s)
@@ -320,15 +353,16 @@ QF_D void tx_convert(const TxParams& P, double2 (&x)[8], unsigned char* sa, int*
       ur[j] = tx_biased(x[j0 + j].x, Ep);
       ui[j] = tx_biased(x[j0 + j].y, Ep);
     }
+    if (nb >= 0) tx_load_half(P, in, x, j0, nb);
     // digit t of amplitudes c = 8 ih + j0 .. + 3: fp16 elements (t & 1) 32 + 2c
     // of chunk t >> 1, one 16-byte piece
 #define QF_TX_STORE(T)                                                                                   \
   {                                                                                                      \
     uint4 v;                                                                                             \
-    v.x = tx_digit_pair<T>(ur[0], ui[0]);                                                               \
-    v.y = tx_digit_pair<T>(ur[1], ui[1]);                                                               \
-    v.z = tx_digit_pair<T>(ur[2], ui[2]);                                                               \
-    v.w = tx_digit_pair<T>(ur[3], ui[3]);                                                               \
+    v.x = tx_digit_pair_a<T>(ur[0], ui[0]);                                                             \
+    v.y = tx_digit_pair_a<T>(ur[1], ui[1]);                                                             \
+    v.z = tx_digit_pair_a<T>(ur[2], ui[2]);                                                             \
+    v.w = tx_digit_pair_a<T>(ur[3], ui[3]);                                                             \
     const int piece = ((T & 1) * 32 + 2 * (8 * ih + j0)) >> 3;                                          \
     *reinterpret_cast<uint4*>(sa + (T >> 1) * TX_A_CHUNK + tx_piece(irow, piece)) = v;                  \
   }
@@ -457,15 +491,13 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   const uint32_t tmem = tmem_slot;
   const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
   if (warp < 8) {
-    // ---- converters and the MMA issuer.  The loads of tile i + 1 are
-    // issued before tile i is converted, into a second register set, so a
-    // whole iteration hides their latency.
+    // ---- converters and the MMA issuer
     const double2* __restrict__ in = static_cast<const double2*>(P.in);
     const uint32_t bbase = tx_smem(sb);
     const int irow = warp * 16 + (lane & 7) + ((lane >> 4) << 3), ih = (lane >> 3) & 1;
     const int64_t hrow = tx_spread(P, irow) | (ih ? P.off[8] : 0);  // this half-row within its tile
     const int64_t step = gridDim.x;
-    double2 x[8], xn[8];
+    double2 x[8];
     int64_t tile = blockIdx.x;
     if (tile < ntiles) {
       const int64_t b = tx_spread(P, tile * TX_ROWS) | hrow;
@@ -475,18 +507,14 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
     int fail = 0;
     for (int it = 0; tile < ntiles; tile += step, ++it) {
       const int s = it & 1;
-      const bool more = tile + step < ntiles;
-      if (more) {
-        const int64_t nb = tx_spread(P, (tile + step) * TX_ROWS) | hrow;
-        tx_load_half(P, in, xn, 0, nb);
-        tx_load_half(P, in, xn, 4, nb);
-      }
       bool ok = true;
       if (it >= 2) ok = tx_wait(&tmem_free[s], static_cast<uint32_t>((it >> 1) - 1) & 1u, P.err);
       if (!__all_sync(0xffffffffu, ok)) fail = 1;  // warp-uniform: the row exponent shuffles within the warp
       tx_fence_after();
       unsigned char* sa = sm + s * TX_A_BYTES;
-      if (!fail) tx_convert(P, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | hrow, irow, ih, tx_rowexp(x));
+      const int64_t nb = tile + step < ntiles ? tx_spread(P, (tile + step) * TX_ROWS) | hrow : -1;
+      if (!fail)
+        tx_convert(P, in, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | hrow, irow, ih, tx_rowexp(x), nb);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (tx_bar_or(1, 256, fail)) break;
       if (tid == 0) {
@@ -494,10 +522,6 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
         tx_fence_after();
         tx_issue(tx_smem(sa), bbase, tmem + static_cast<uint32_t>(256 * s));
         tx_commit(&mma_done[s]);
-      }
-      if (more) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = xn[j];
       }
     }
   } else {
