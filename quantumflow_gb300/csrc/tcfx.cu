@@ -236,23 +236,26 @@ QF_D uint32_t tx_digit_pair_a(uint64_t x, uint64_t y) {
 
 // Z = sum_delta acc_delta 2^(49 - 8 delta) (= A.G / 2^63) from the eight
 // accumulator words (FP32 integers below 2^22): each becomes 1.5 * 2^23 +
-// acc exactly, whose bit pattern is TX_MAGIC_BITS + acc; pairs are joined in
-// int32 (acc_2j 2^8 + acc_2j+1 < 2^31) and the biases cancel in one
-// constant.  The shifts and adds are multiply-adds (the FMA pipe), the
-// integer ALU being the busiest unit of this kernel.
+// acc exactly, whose bit pattern is TX_MAGIC_BITS + acc.  A pair joins in
+// uint32 as b_2j 256 + b_2j+1 = p_j + K2 with p_j = acc_2j 256 + acc_2j+1
+// (|p_j| < 2^30 + 2^22) and K2 = 257 TX_MAGIC_BITS mod 2^32 = 0x8B400000,
+// which never wraps; K2 is a multiple of 128, so the biases of the four
+// pairs leave one constant, subtracted once.  The shifts and adds are
+// multiply-adds (the FMA pipe), the integer ALU being the busiest unit.
 QF_D int64_t tx_combine(const uint32_t (&w)[8]) {
   uint32_t b[8];
 #pragma unroll
   for (int d = 0; d < 8; ++d) b[d] = __float_as_uint(__uint_as_float(w[d]) + TX_MAGIC);
-  constexpr uint32_t K2 = static_cast<uint32_t>(TX_MAGIC_BITS) * 257u;  // bias of one joined pair (mod 2^32)
-  const int32_t p0 = static_cast<int32_t>(b[0] * 256u + b[1] - K2);
-  const int32_t p1 = static_cast<int32_t>(b[2] * 256u + b[3] - K2);
-  const int32_t p2 = static_cast<int32_t>(b[4] * 256u + b[5] - K2);
-  const int32_t p3 = static_cast<int32_t>(b[6] * 256u + b[7] - K2);
-  // two's complement sums wrap mod 2^64; the true Z fits int64
-  int64_t z = fx_mad(p2, 1 << 9, static_cast<int64_t>(p3 >> 7));
-  z = fx_mad(p1, 1 << 25, z);
-  const uint32_t zh = static_cast<uint32_t>(static_cast<uint64_t>(z) >> 32) + static_cast<uint32_t>(p0) * 512u;
+  constexpr uint32_t K2 = static_cast<uint32_t>(TX_MAGIC_BITS) * 257u;
+  static_assert(K2 == 0x8B400000u && K2 % 128u == 0u, "pair bias");
+  constexpr uint64_t C = (static_cast<uint64_t>(K2) << 41) + (static_cast<uint64_t>(K2) << 25) +
+                         (static_cast<uint64_t>(K2) << 9) + (K2 >> 7);
+  const uint32_t q0 = b[0] * 256u + b[1], q1 = b[2] * 256u + b[3];
+  const uint32_t q2 = b[4] * 256u + b[5], q3 = b[6] * 256u + b[7];
+  // sums wrap mod 2^64; the true Z fits int64
+  uint64_t z = fx_madu(q2, 1u << 9, static_cast<uint64_t>(q3 >> 7) - C);
+  z = fx_madu(q1, 1u << 25, z);
+  const uint32_t zh = static_cast<uint32_t>(z >> 32) + q0 * 512u;
   return static_cast<int64_t>((static_cast<uint64_t>(zh) << 32) | static_cast<uint32_t>(z));
 }
 
@@ -440,26 +443,15 @@ QF_D void tx_bar_init(uint64_t* bar, uint32_t count) {
 QF_D void tx_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tx_smem(bar)) : "memory");
 }
-// barrier `id` over `count` threads, returning whether any of them passed v != 0
-QF_D int tx_bar_or(int id, int count, int v) {
-  int r;
-  asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\t"
-      "barrier.cta.red.or.pred q, %2, %3, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
-      : "=r"(r)
-      : "r"(v), "r"(id), "r"(count)
-      : "memory");
-  return r;
-}
 
 // ------------------------------------------------ warp-specialised kernel ----
 // One CTA of 512 threads per SM, two stages of A, rowE and accumulators.
 // Warps 0-7 convert tile i into stage i & 1 (after the epilogue of tile
-// i - 2 released it), meet at a named barrier, and thread 0 marks the
-// stage's row exponents written (conv_done) and issues the tile's MMAs,
-// committed to mma_done[stage].  Warps 8-15 wait for both, run the
-// epilogue from the stage's accumulators and release the stage (tmem_free,
-// one arrival per warp).  Conversion of one tile, the MMAs of
+// i - 2 released it) and arrive on a_full[stage]; thread 0 waits for all
+// 256 arrivals and issues the tile's MMAs, committed to mma_done[stage],
+// while warps 1-7 go on with their next tile.  Warps 8-15 wait for both
+// barriers, run the epilogue from the stage's accumulators and release the
+// stage (tmem_free, one arrival per warp).  Conversion of one tile, the MMAs of
 // the next and the epilogue of the one before run at the same time.
 constexpr int TP_THREADS = 512;
 constexpr uint32_t TP_SMEM = 2 * TX_A_BYTES + TX_B_BYTES + 1024;
@@ -469,7 +461,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   extern __shared__ __align__(1024) unsigned char tx_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tx_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* sb = sm + 2 * TX_A_BYTES;
-  __shared__ __align__(8) uint64_t mma_done[2], conv_done[2], tmem_free[2];
+  __shared__ __align__(8) uint64_t mma_done[2], a_full[2], tmem_free[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int rowE[2][TX_ROWS];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -478,8 +470,8 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   if (tid == 0) {
     tx_bar_init(&mma_done[0], 1);
     tx_bar_init(&mma_done[1], 1);
-    tx_bar_init(&conv_done[0], 1);
-    tx_bar_init(&conv_done[1], 1);
+    tx_bar_init(&a_full[0], 256);
+    tx_bar_init(&a_full[1], 256);
     tx_bar_init(&tmem_free[0], 8);
     tx_bar_init(&tmem_free[1], 8);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -515,13 +507,20 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
       const int64_t nb = tile + step < ntiles ? tx_spread(P, (tile + step) * TX_ROWS) | hrow : -1;
       if (!fail)
         tx_convert(P, in, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | hrow, irow, ih, tx_rowexp(x), nb);
+      if (fail) break;
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      if (tx_bar_or(1, 256, fail)) break;
-      if (tid == 0) {
-        tx_arrive(&conv_done[s]);  // the row exponents of this stage are written
-        tx_fence_after();
-        tx_issue(tx_smem(sa), bbase, tmem + static_cast<uint32_t>(256 * s));
-        tx_commit(&mma_done[s]);
+      tx_arrive(&a_full[s]);  // this thread's digits and row exponent are written
+      if (warp == 0) {
+        // warp 0 issues the tile's MMAs once every converter has arrived; the
+        // other converter warps go straight on to their next tile
+        bool issued = false;
+        if (lane == 0 && tx_wait(&a_full[s], static_cast<uint32_t>(it >> 1) & 1u, P.err)) {
+          tx_fence_after();
+          tx_issue(tx_smem(sa), bbase, tmem + static_cast<uint32_t>(256 * s));
+          tx_commit(&mma_done[s]);
+          issued = true;
+        }
+        if (!__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) break;
       }
     }
   } else {
@@ -535,7 +534,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
     for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
       const int s = it & 1;
       const uint32_t par = static_cast<uint32_t>(it >> 1) & 1u;
-      const bool ok = tx_wait(&conv_done[s], par, P.err) && tx_wait(&mma_done[s], par, P.err);
+      const bool ok = tx_wait(&a_full[s], par, P.err) && tx_wait(&mma_done[s], par, P.err);
       if (!__all_sync(0xffffffffu, ok)) break;
       tx_fence_after();
       tx_epilogue(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * s), rowE[s][orow],
