@@ -305,59 +305,60 @@ QF_D int64_t tx_spread(const TxParams& P, int64_t x) {
   return x;
 }
 
-// the amplitudes j0 .. j0 + 3 of a thread's half-row (base b: the row's
-// base with the half's window bit already set)
-QF_D void tx_load_half(const TxParams& P, const double2* __restrict__ in, double2 (&x)[8], int j0, int64_t b) {
-#pragma unroll
-  for (int j = 0; j < 4; ++j) x[j0 + j] = in[b | P.off[j0 + j]];
-}
 
-// Row exponent of a thread's half-row and its partner's (lane ^ 8): the
-// largest FP64 exponent field (4095 for rows below 2^-959, which become 0).
-QF_D int tx_rowexp(const double2 (&x)[8]) {
+// Row exponent shared by the AP-amplitude groups of one row (lanes l, l ^ 8
+// and, for AP = 4, l ^ 16, l ^ 24): the largest FP64 exponent field (4095
+// for rows below 2^-959, which become 0).
+template <int AP>
+QF_D int tx_rowexp(const double2 (&x)[AP]) {
   uint32_t mx = 0u;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < AP; ++j) {
     mx = max(mx, fx_hiword(x[j].x) & 0x7fffffffu);
     mx = max(mx, fx_hiword(x[j].y) & 0x7fffffffu);
   }
   mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 8));
+  if (AP == 4) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
   return static_cast<int>(mx >> 20) < FX_EMIN ? 4095 : static_cast<int>(mx >> 20);
 }
 
-// Input half-row of one thread: its 8 amplitudes (window indices 8 ih + j)
+// Input group of one thread: its AP amplitudes (window indices AP q + j)
 // of row irow, after the input-side signs, become digits in A (sa), scaled
 // by the row exponent E (tx_rowexp), which goes to rowE[irow].  b is the
-// half-row's base (the input-side signs test it).  As soon as a group of
-// four amplitudes has become integers, its registers take the loads of the
-// same amplitudes of the next tile (half-row base nb; none when nb < 0), so
-// those are in flight during the rest of this conversion and the MMAs.
-QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 (&x)[8], unsigned char* sa,
-                     int* rowE, int64_t b, int irow, int ih, int E, int64_t nb) {
+// group's base (the input-side signs test it).  As soon as four amplitudes
+// have become integers, their registers take the loads of the same
+// amplitudes of the next tile (group base nb; none when nb < 0), so those
+// are in flight during the rest of this conversion and the MMAs.
+template <int AP>
+QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 (&x)[AP], unsigned char* sa,
+                     int* rowE, int64_t b, int irow, int q, int E, int64_t nb) {
   if (P.nin > 0) {
     uint32_t fl = 0u;
     for (int s = 0; s < P.nin; ++s)
       if ((static_cast<uint64_t>(b) & P.in_mout[s]) == P.in_mout[s]) fl ^= P.in_rmask[s];
-    fl = (fl >> (8 * ih)) & 0xFFu;
+    fl >>= AP * q;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < AP; ++j) {
       const uint32_t sg = ((fl >> j) & 1u) << 31;
       x[j] = make_double2(fx_double(fx_hiword(x[j].x) ^ sg, fx_loword(x[j].x)),
                           fx_double(fx_hiword(x[j].y) ^ sg, fx_loword(x[j].y)));
     }
   }
-  if (ih == 0) rowE[irow] = E;
+  if (q == 0) rowE[irow] = E;
   const uint32_t Ep = static_cast<uint32_t>(E + 64 - TX_MB);
 #pragma unroll
-  for (int j0 = 0; j0 < 8; j0 += 4) {
+  for (int j0 = 0; j0 < AP; j0 += 4) {
     uint64_t ur[4], ui[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       ur[j] = tx_biased(x[j0 + j].x, Ep);
       ui[j] = tx_biased(x[j0 + j].y, Ep);
     }
-    if (nb >= 0) tx_load_half(P, in, x, j0, nb);
-    // digit t of amplitudes c = 8 ih + j0 .. + 3: fp16 elements (t & 1) 32 + 2c
+    if (nb >= 0) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) x[j0 + j] = in[nb | P.off[j0 + j]];
+    }
+    // digit t of amplitudes c = AP q + j0 .. + 3: fp16 elements (t & 1) 32 + 2c
     // of chunk t >> 1, one 16-byte piece
 #define QF_TX_STORE(T)                                                                                   \
   {                                                                                                      \
@@ -366,7 +367,7 @@ QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 
     v.y = tx_digit_pair_a<T>(ur[1], ui[1]);                                                             \
     v.z = tx_digit_pair_a<T>(ur[2], ui[2]);                                                             \
     v.w = tx_digit_pair_a<T>(ur[3], ui[3]);                                                             \
-    const int piece = ((T & 1) * 32 + 2 * (8 * ih + j0)) >> 3;                                          \
+    const int piece = ((T & 1) * 32 + 2 * (AP * q + j0)) >> 3;                                          \
     *reinterpret_cast<uint4*>(sa + (T >> 1) * TX_A_CHUNK + tx_piece(irow, piece)) = v;                  \
   }
     QF_TX_STORE(0)
@@ -400,22 +401,27 @@ QF_D void tx_issue(uint32_t abase, uint32_t bbase, uint32_t acc) {
 // row (half-row base b) from the accumulators at tensor-memory address acc
 // (lane field set), with the output-side signs, stored as FP64.  The tensor-memory loads of
 // the next four reals are in flight while four are converted.
+template <bool DB>
 QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int64_t b, int oh) {
   const uint32_t delta = static_cast<uint32_t>(E - 1082) << 20;
   uint32_t fl = 0u;
   for (int s = 0; s < P.nout; ++s)
     if ((static_cast<uint64_t>(b) & P.out_mout[s]) == P.out_mout[s]) fl ^= P.out_rmask[s];
   fl = (fl >> (8 * oh)) & 0xFFu;
-  uint32_t a4[2][8][4];
+  uint32_t a4[DB ? 2 : 1][8][4];
 #pragma unroll
   for (int d = 0; d < 8; ++d) tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh), a4[0][d]);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    tx_wait_ld(a4[q & 1]);
-    if (q < 3) {
+    if (!DB && q > 0) {
+#pragma unroll
+      for (int d = 0; d < 8; ++d) tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh + 4 * q), a4[0][d]);
+    }
+    tx_wait_ld(a4[DB ? (q & 1) : 0]);
+    if (DB && q < 3) {
 #pragma unroll
       for (int d = 0; d < 8; ++d)
-        tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh + 4 * (q + 1)), a4[(q + 1) & 1][d]);
+        tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh + 4 * (q + 1)), a4[DB ? ((q + 1) & 1) : 0][d]);
     }
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
@@ -423,8 +429,8 @@ QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int6
       uint32_t wr[8], wi[8];
 #pragma unroll
       for (int d = 0; d < 8; ++d) {
-        wr[d] = a4[q & 1][d][2 * a];
-        wi[d] = a4[q & 1][d][2 * a + 1];
+        wr[d] = a4[DB ? (q & 1) : 0][d][2 * a];
+        wi[d] = a4[DB ? (q & 1) : 0][d][2 * a + 1];
       }
       const uint32_t sg = ((fl >> j) & 1u) << 31;
       out[b | P.off[j]] = make_double2(tx_out(tx_combine(wr), delta, sg), tx_out(tx_combine(wi), delta, sg));
@@ -445,19 +451,27 @@ QF_D void tx_arrive(uint64_t* bar) {
 }
 
 // ------------------------------------------------ warp-specialised kernel ----
-// One CTA of 512 threads per SM, two stages of A, rowE and accumulators.
-// Warps 0-7 convert tile i into stage i & 1 (after the epilogue of tile
-// i - 2 released it) and arrive on a_full[stage]; thread 0 waits for all
-// 256 arrivals and issues the tile's MMAs, committed to mma_done[stage],
-// while warps 1-7 go on with their next tile.  Warps 8-15 wait for both
+// One CTA per SM, two stages of A, rowE and accumulators.  The converter
+// warps (AP amplitudes per thread: 8 -> 8 warps, 4 -> 16 warps) convert
+// tile i into stage i & 1 (after the epilogue of tile i - 2 released it)
+// and arrive on a_full[stage]; thread 0 waits for all of them and issues
+// the tile's MMAs, committed to mma_done[stage], while the other converter
+// warps go on with their next tile.  The 8 epilogue warps wait for both
 // barriers, run the epilogue from the stage's accumulators and release the
-// stage (tmem_free, one arrival per warp).  Conversion of one tile, the MMAs of
-// the next and the epilogue of the one before run at the same time.
-constexpr int TP_THREADS = 512;
+// stage (tmem_free, one arrival per warp).
 constexpr uint32_t TP_SMEM = 2 * TX_A_BYTES + TX_B_BYTES + 1024;
 constexpr int TP_TMEM_COLS = 512;
 
-__global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant__ TxParams P) {
+template <int AP>
+struct TxShape {
+  static constexpr int CW = 128 * (16 / AP) / 32;  // converter warps
+  static constexpr int THREADS = 32 * (CW + 8);
+  static constexpr bool DB = AP == 8;               // double-buffered tensor-memory reads (registers allow)
+};
+
+template <int AP>
+__global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid_constant__ TxParams P) {
+  constexpr int CW = TxShape<AP>::CW;
   extern __shared__ __align__(1024) unsigned char tx_raw[];
   unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tx_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* sb = sm + 2 * TX_A_BYTES;
@@ -465,13 +479,13 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   __shared__ uint32_t tmem_slot;
   __shared__ int rowE[2][TX_ROWS];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  tx_build_b(P, sb, tid, TP_THREADS);
+  tx_build_b(P, sb, tid, TxShape<AP>::THREADS);
   if (warp == 0) tx_alloc(&tmem_slot, TP_TMEM_COLS);
   if (tid == 0) {
     tx_bar_init(&mma_done[0], 1);
     tx_bar_init(&mma_done[1], 1);
-    tx_bar_init(&a_full[0], 256);
-    tx_bar_init(&a_full[1], 256);
+    tx_bar_init(&a_full[0], 32 * CW);
+    tx_bar_init(&a_full[1], 32 * CW);
     tx_bar_init(&tmem_free[0], 8);
     tx_bar_init(&tmem_free[1], 8);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -482,19 +496,23 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   tx_fence_after();
   const uint32_t tmem = tmem_slot;
   const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
-  if (warp < 8) {
-    // ---- converters and the MMA issuer
+  if (warp < CW) {
+    // ---- converters and the MMA issuer.  Row irow, group q (window
+    // indices AP q .. AP q + AP - 1); the lanes of one 8-lane shared-store
+    // phase hold 8 consecutive rows (distinct swizzle phases) and the groups
+    // of a row are lanes l ^ 8 (and l ^ 16, l ^ 24)
     const double2* __restrict__ in = static_cast<const double2*>(P.in);
     const uint32_t bbase = tx_smem(sb);
-    const int irow = warp * 16 + (lane & 7) + ((lane >> 4) << 3), ih = (lane >> 3) & 1;
-    const int64_t hrow = tx_spread(P, irow) | (ih ? P.off[8] : 0);  // this half-row within its tile
+    const int irow = AP == 8 ? warp * 16 + (lane & 7) + ((lane >> 4) << 3) : warp * 8 + (lane & 7);
+    const int q = AP == 8 ? (lane >> 3) & 1 : lane >> 3;
+    const int64_t grow = tx_spread(P, irow) | P.off[AP * q];  // this group within its tile
     const int64_t step = gridDim.x;
-    double2 x[8];
+    double2 x[AP];
     int64_t tile = blockIdx.x;
     if (tile < ntiles) {
-      const int64_t b = tx_spread(P, tile * TX_ROWS) | hrow;
-      tx_load_half(P, in, x, 0, b);
-      tx_load_half(P, in, x, 4, b);
+      const int64_t b = tx_spread(P, tile * TX_ROWS) | grow;
+#pragma unroll
+      for (int j = 0; j < AP; ++j) x[j] = in[b | P.off[j]];
     }
     int fail = 0;
     for (int it = 0; tile < ntiles; tile += step, ++it) {
@@ -504,9 +522,9 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
       if (!__all_sync(0xffffffffu, ok)) fail = 1;  // warp-uniform: the row exponent shuffles within the warp
       tx_fence_after();
       unsigned char* sa = sm + s * TX_A_BYTES;
-      const int64_t nb = tile + step < ntiles ? tx_spread(P, (tile + step) * TX_ROWS) | hrow : -1;
+      const int64_t nb = tile + step < ntiles ? tx_spread(P, (tile + step) * TX_ROWS) | grow : -1;
       if (!fail)
-        tx_convert(P, in, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | hrow, irow, ih, tx_rowexp(x), nb);
+        tx_convert<AP>(P, in, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | grow, irow, q, tx_rowexp<AP>(x), nb);
       if (fail) break;
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tx_arrive(&a_full[s]);  // this thread's digits and row exponent are written
@@ -526,7 +544,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
   } else {
     // ---- epilogue
     double2* out = static_cast<double2*>(P.out);
-    const int ew = warp - 8;
+    const int ew = warp - CW;
     const int orow = 32 * (ew & 3) + lane, oh = ew >> 2;
     const int64_t hrow = tx_spread(P, orow) | (oh ? P.off[8] : 0);
     const uint32_t lane_addr = static_cast<uint32_t>(32 * (ew & 3)) << 16;
@@ -537,8 +555,8 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
       const bool ok = tx_wait(&a_full[s], par, P.err) && tx_wait(&mma_done[s], par, P.err);
       if (!__all_sync(0xffffffffu, ok)) break;
       tx_fence_after();
-      tx_epilogue(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * s), rowE[s][orow],
-                  tx_spread(P, tile * TX_ROWS) | hrow, oh);
+      tx_epilogue<TxShape<AP>::DB>(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * s), rowE[s][orow],
+                                   tx_spread(P, tile * TX_ROWS) | hrow, oh);
       tx_fence_before();
       __syncwarp();
       if (lane == 0) tx_arrive(&tmem_free[s]);
@@ -550,6 +568,23 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP_TMEM_COLS) : "memory");
 }
 
+template <int AP>
+int tx_launch_ap(const TxParams& P, cudaStream_t stream) {
+  static std::atomic<int> attr_set[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!attr_set[dev].load()) {
+    int rc = check_cuda(cudaFuncSetAttribute(k_txpipe<AP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TP_SMEM));
+    if (rc) return rc;
+    attr_set[dev].store(1);
+  }
+  const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
+  int64_t grid = device_sm_count();
+  if (grid > ntiles) grid = ntiles;
+  k_txpipe<AP><<<(int)grid, TxShape<AP>::THREADS, TP_SMEM, stream>>>(P);
+  return check_cuda(cudaGetLastError());
+}
+
 }  // namespace
 
 // Launch one tensor-core pass (P.in/out/err set by the caller); the state
@@ -557,19 +592,10 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_txpipe(const __grid_constant_
 // its outputs are written, by the same CTA, so the pass may run in place.
 int tx_launch(const TxParams& P, cudaStream_t stream) {
   if (P.n < 11) return QF_ERR_NOT_SUPPORTED;
-  static std::atomic<int> attr_set[64];
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
-  if (!attr_set[dev].load()) {
-    int rc = check_cuda(cudaFuncSetAttribute(k_txpipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TP_SMEM));
-    if (rc) return rc;
-    attr_set[dev].store(1);
-  }
-  const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
-  int64_t grid = device_sm_count();
-  if (grid > ntiles) grid = ntiles;
-  k_txpipe<<<(int)grid, TP_THREADS, TP_SMEM, stream>>>(P);
-  return check_cuda(cudaGetLastError());
+  // eight amplitudes per converter thread: 8 converter warps at 128
+  // registers; four per thread (16 converter warps, 80 registers) issued 12%
+  // more instructions and ran 7% slower at N=28
+  return tx_launch_ap<8>(P, stream);
 }
 
 }  // namespace qf
