@@ -259,15 +259,16 @@ QF_D int64_t tx_combine(const uint32_t (&w)[8]) {
   return static_cast<int64_t>((static_cast<uint64_t>(zh) << 32) | static_cast<uint32_t>(z));
 }
 
-// FP64 value of Z * 2^(E - 1082), its sign flipped when sg is the sign
-// bit: Z is converted exactly rounded by the FP64 pipe's convert, and the
-// power of two (delta = (E - 1082) << 20) and the sign flip (adding 2^31
-// mod 2^32) are one add on the high word.  E >= 64 and |Z| >= 1 keep the
-// result normal; Z = 0 gives 0.
-QF_D double tx_out(int64_t Z, uint32_t delta, uint32_t sg) {
+// FP64 value of Z * 2^(E - 1082), its sign flipped when the sign bit of ds
+// is set: Z is converted exactly rounded by the FP64 pipe's convert, and
+// the power of two (delta = (E - 1082) << 20) and the sign flip (adding
+// 2^31 mod 2^32) are one multiply-add on the high word, ds = delta ^ sign,
+// scaled by min(hi, 1) so that Z = 0 stays 0 without a compare and select
+// on the integer ALU.  E >= 64 and |Z| >= 1 keep the result normal.
+QF_D double tx_out(int64_t Z, uint32_t ds) {
   const double d = __ll2double_rn(Z);
   const uint32_t hi = fx_hiword(d);
-  return fx_double(hi != 0u ? hi + delta + sg : 0u, fx_loword(d));
+  return fx_double(hi + min(hi, 1u) * ds, fx_loword(d));
 }
 
 // ------------------------------------------------------------ pass parts ----
@@ -432,8 +433,8 @@ QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int6
         wr[d] = a4[DB ? (q & 1) : 0][d][2 * a];
         wi[d] = a4[DB ? (q & 1) : 0][d][2 * a + 1];
       }
-      const uint32_t sg = ((fl >> j) & 1u) << 31;
-      out[b | P.off[j]] = make_double2(tx_out(tx_combine(wr), delta, sg), tx_out(tx_combine(wi), delta, sg));
+      const uint32_t ds = delta ^ (((fl >> j) & 1u) << 31);
+      out[b | P.off[j]] = make_double2(tx_out(tx_combine(wr), ds), tx_out(tx_combine(wi), ds));
     }
   }
 }
