@@ -3,7 +3,8 @@ complex128 states of at least 2^11 amplitudes): bit-for-bit agreement with
 the CPU model of the digit arithmetic (tests/txarith.py), parity with the
 oracle (the reference's numpy backend restated) at 1e-12 on circuits with
 every op class the pass takes, sign ops on both sides of the gates, in and
-out of place, and the planner's routing."""
+out of place.  The planner's routing is tested on the CPU
+(tests/test_tensor_fx_plan.py)."""
 import numpy as np
 import pytest
 import torch
@@ -152,34 +153,3 @@ def test_fused_circuits_against_oracle(tensor_cores, N, fusion_k, monkeypatch):
     tensor_cores.call("qf_set_fx_tensor_cores", 0)
     alt = circ.run(qf.zero_state(N), fusion_k=fusion_k).asarray().reshape(-1)
     assert float(np.max(np.abs(alt - ref))) < TOL
-
-
-def test_plan_routes_fused_passes_to_tensor_cores(tensor_cores):
-    """The merged random-layer circuit at N=20: every fused pass of dense
-    gates and signs is a tensor-core pass; with the switch off none is."""
-    import quantumflow_gb300 as qf
-    nat = tensor_cores
-    rng = np.random.default_rng(5)
-    N = 20
-    circ = qf.Circuit()
-    for _ in range(4):
-        for q in range(N):
-            circ += qf.random_gate([q], random_state=rng)
-        perm = rng.permutation(N)
-        for a in range(0, N - 1, 2):
-            circ += qf.CZ(int(perm[a]), int(perm[a + 1]))
-    op_k, op_axes, op_mats, nops = circ.packed(tuple(range(N)))
-
-    def kinds():
-        stats = (nat.ctypes.c_int32 * (8 * 4096))()
-        nb = nat.ctypes.c_int(0)
-        nat.call("qf_plan_circuit", N, nat.LAYOUT_FX, nops, op_k.ctypes.data_as(nat._ip),
-                 op_axes.ctypes.data_as(nat._ip), op_mats.ctypes.data_as(nat._dp), 0, stats, 4096,
-                 nat.ctypes.byref(nb))
-        return [stats[8 * b + 7] for b in range(nb.value)]
-    k_on = kinds()
-    assert set(k_on) == {6}, k_on
-    nat.call("qf_set_fx_tensor_cores", 0)
-    k_off = kinds()
-    assert 6 not in k_off and len(k_off) >= len(k_on)
-
