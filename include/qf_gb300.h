@@ -25,12 +25,14 @@
  *                   (re_hi, re_lo, im_hi, im_lo), 48-bit significand,
  *                   float-float math on the FP32 pipes            16
  *   QF_LAYOUT_FX    complex128 (double re, double im), the same bytes as
- *                   QF_LAYOUT_C128; gates computed in 64-bit integer
- *                   fixed point (each thread's amplitude group shares one
- *                   exponent, >= 55 significant bits relative to the
- *                   group's largest part, one FP64 rounding per pass).
- *                   Unitary gates only take this arithmetic; other gates,
- *                   and every entry point other than qf_apply_gate /
+ *                   QF_LAYOUT_C128; gates computed in fixed point: fused
+ *                   passes as 61-bit integer digits on the tensor cores
+ *                   (qf_set_fx_tensor_cores), the rest in 64-bit integer
+ *                   arithmetic on the CUDA cores (each amplitude group
+ *                   shares one exponent, >= 55 significant bits relative
+ *                   to the group's largest part, one FP64 rounding per
+ *                   pass).  Unitary gates only take this arithmetic; other
+ *                   gates, and every entry point other than qf_apply_gate /
  *                   qf_run_circuit / qf_plan_circuit, treat the buffer as
  *                   QF_LAYOUT_C128 (native FP64)                  16
  */
@@ -178,10 +180,11 @@ int qf_set_dense_tensor_cores(int on);
 int qf_set_fx_occupancy(int min_blocks);
 /* Complex128 (QF_LAYOUT_FX) fused passes on the tensor cores (default 1):
  * a pass of unitary gates on at most four bits, with CZ-like signs around
- * them, runs as one 16 x 16 unitary applied by fp16 tcgen05 MMAs to
- * base-256 integer digits of a 60-bit fixed-point form of each row of 16
- * amplitudes (exact FP32 accumulation, one FP64 rounding per pass; states
- * of at least 2^11 amplitudes); 0 = the CUDA-core fixed-point kernels.
+ * them, or one unitary gate on 3 or 4 qubits, runs as one 16 x 16 unitary
+ * applied by fp16 tcgen05 MMAs to base-256 integer digits of a 61-bit
+ * fixed-point form of each row of 16 amplitudes (exact FP32 accumulation,
+ * one FP64 rounding per pass; states of at least 2^11 amplitudes); 0 = the
+ * CUDA-core fixed-point kernels (3- and 4-qubit gates in native FP64).
  * Process-wide; no reference counterpart. */
 int qf_set_fx_tensor_cores(int on);
 

@@ -633,9 +633,23 @@ struct FxBlock {
   int order[4] = {0, 0, 0, 0};  // dense bits in order of first use
   int G = 0;
   bool native = false;  // one op run by the native FP64 kernels
+  bool wide = false;    // one unitary gate on 3 or 4 qubits for the tensor-core pass
   int ncoef = 0;
   int shape = -1;       // table shape of a straight-line pass (-1: other kernels)
 };
+
+// A unitary gate on 3 or 4 qubits (dense, or a generalised permutation
+// with unit-modulus entries on 3): the CUDA-core fixed-point kernels do not
+// take it, but it is one 16x16 window of the tensor-core pass.
+bool tx_wide(const HostOp& op) {
+  if (op.type == OP_DENSEK) return op.k <= 4 && unitary(op.m, 1 << op.k);
+  if (op.type == OP_MONO && op.k == 3) {
+    for (int r = 0; r < 8; ++r)
+      if (!unit_modulus(op.diag[r])) return false;
+    return true;
+  }
+  return false;
+}
 
 constexpr int FX_G_MAX = 4;
 
@@ -644,7 +658,8 @@ constexpr int FX_G_MAX = 4;
 // do not take close the pass and run alone in native FP64.
 std::vector<FxBlock> fx_split_shapes(std::vector<FxBlock>& blocks, const std::vector<HostOp>& ops);
 
-std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k, bool split = true) {
+std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k, bool split = true,
+                             bool wide_ok = false) {
   if (fusion_k <= 0) fusion_k = FX_G_MAX;
   if (fusion_k > 1 && g_merge_gates) merge_ops(ops, n);
   // generalised permutations on <= 2 qubits with unit-modulus entries run as
@@ -669,7 +684,13 @@ std::vector<FxBlock> fx_plan(std::vector<HostOp>& ops, int n, int& fusion_k, boo
     if (kind == FXK_NATIVE) {
       close();
       cur.idx.push_back(i);
-      cur.native = true;
+      if (wide_ok && tx_wide(op)) {
+        cur.wide = true;
+        cur.G = op.k;
+        for (int j = 0; j < op.k; ++j) cur.order[j] = op.gb[j];
+      } else {
+        cur.native = true;
+      }
       close();
       continue;
     }
@@ -1035,6 +1056,9 @@ int fx_shape_launch(const FxShapeParams& P, cudaStream_t stream) {
 // touches its window bits, else to the outputs when no later one does.
 int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams& P) {
   if (B.native || B.G < 1 || B.G > 4 || n < 11) return QF_ERR_NOT_SUPPORTED;
+  auto dense_op = [](const HostOp& op) {
+    return op.type == OP_DENSE1 || op.type == OP_DENSE2 || op.type == OP_DENSEK || op.type == OP_MONO;
+  };
   using lcplx = std::complex<long double>;
   int wb[4], nw = 0;
   for (int j = 0; j < B.G; ++j) wb[nw++] = B.order[j];
@@ -1065,7 +1089,7 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
   std::vector<uint32_t> dense_bits;
   for (int k = 0; k < (int)B.idx.size(); ++k) {
     const HostOp& op = ops[B.idx[k]];
-    if (op.type == OP_DENSE1 || op.type == OP_DENSE2) {
+    if (dense_op(op)) {
       uint32_t m = 0;
       for (int j = 0; j < op.k; ++j) m |= 1u << pos(op.gb[j]);
       dense_pos.push_back(k);
@@ -1074,11 +1098,15 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
   }
   for (int k = 0; k < (int)B.idx.size(); ++k) {
     const HostOp& op = ops[B.idx[k]];
-    if (fx_kind(op) == FXK_NATIVE) return QF_ERR_NOT_SUPPORTED;
-    if (op.type == OP_DENSE1 || op.type == OP_DENSE2) {
-      int jp[2];
-      for (int j = 0; j < op.k; ++j) jp[j] = pos(op.gb[j]);
+    if (fx_kind(op) == FXK_NATIVE && !tx_wide(op)) return QF_ERR_NOT_SUPPORTED;
+    if (dense_op(op)) {
+      int jp[4];
+      for (int j = 0; j < op.k; ++j) {
+        jp[j] = pos(op.gb[j]);
+        if (jp[j] < 0) return QF_ERR_NOT_SUPPORTED;
+      }
       const int D = 1 << op.k;
+      const std::vector<cplx> gm = dense_matrix(op);
       uint32_t om = 0;
       for (int j = 0; j < op.k; ++j) om |= 1u << jp[j];
       auto local = [&](int c) {  // the gate's matrix index of window index c (gate qubit 0 = MSB)
@@ -1095,7 +1123,7 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
             int cm = r & ~static_cast<int>(om);
             for (int j = 0; j < op.k; ++j)
               if ((m >> (op.k - 1 - j)) & 1) cm |= 1 << jp[j];
-            const cplx g = op.m[lr * D + m];
+            const cplx g = gm[lr * D + m];
             acc += lcplx(g.real(), g.imag()) * U[cm * 16 + c];
           }
           T[r * 16 + c] = acc;
@@ -1174,11 +1202,17 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
 // -2), the others are cut into straight-line shapes as before.
 std::vector<FxBlock> fx_plan_final(std::vector<HostOp>& ops, int n, int& fusion_k) {
   if (!g_fx_tensor || n < 11) return fx_plan(ops, n, fusion_k);
-  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k, false);
+  std::vector<FxBlock> blocks = fx_plan(ops, n, fusion_k, false, true);
   std::vector<FxBlock> out;
   out.reserve(blocks.size());
   static thread_local TxParams tp;  // ~5 KiB: kept off the stack
   for (FxBlock& B : blocks) {
+    if (B.wide) {  // a 3- or 4-qubit gate: alone on the tensor cores, else native FP64
+      if (tx_prepare(n, ops, B, tp) == QF_OK) B.shape = -2;
+      else B.native = true;
+      out.push_back(std::move(B));
+      continue;
+    }
     // a lone 2x2 gate streams faster through the CUDA-core sweep
     const bool lone2x2 = B.idx.size() == 1 && ops[B.idx[0]].type == OP_DENSE1;
     if (!lone2x2 && tx_prepare(n, ops, B, tp) == QF_OK) {

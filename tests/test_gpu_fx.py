@@ -52,8 +52,9 @@ def test_fx_mixed_circuits_against_oracle(N, fusion_k, monkeypatch):
 
 
 def test_fx_plan_uses_fixed_point_passes():
-    """The planner's view of a merged random-layer circuit: group passes of
-    at most four gate bits, no native-FP64 pass for unitary gates."""
+    """The planner's view of a merged random-layer circuit: passes of at
+    most four gate bits, no native-FP64 pass for unitary gates (with the
+    tensor cores off, the 3-qubit permutations run natively)."""
     import quantumflow_gb300 as qf
     from quantumflow_gb300 import _native as nat
     rng = np.random.default_rng(5)
@@ -66,10 +67,21 @@ def test_fx_plan_uses_fixed_point_passes():
              op_axes.ctypes.data_as(nat._ip), op_mats.ctypes.data_as(nat._dp), 0, stats, 4096,
              nat.ctypes.byref(nb))
     kinds = [stats[8 * b + 7] for b in range(nb.value)]
-    # CCNOT (3-qubit permutation) is the one op class that runs natively
-    assert kinds.count(5) == 3
-    assert set(kinds) <= {0, 1, 3, 4, 5, 6}
+    # CCNOT (a 3-qubit permutation) takes a tensor-core window of its own
+    assert kinds.count(5) == 0
+    assert set(kinds) <= {0, 1, 3, 4, 6}
     assert nb.value < nops
+    # with the tensor cores off it is the one op class that runs natively
+    nat.call("qf_set_fx_tensor_cores", 0)
+    try:
+        nat.call("qf_plan_circuit", N, nat.LAYOUT_FX, nops, op_k.ctypes.data_as(nat._ip),
+                 op_axes.ctypes.data_as(nat._ip), op_mats.ctypes.data_as(nat._dp), 0, stats, 4096,
+                 nat.ctypes.byref(nb))
+    finally:
+        nat.call("qf_set_fx_tensor_cores", 1)
+    kinds = [stats[8 * b + 7] for b in range(nb.value)]
+    assert kinds.count(5) == 3
+    assert set(kinds) <= {0, 1, 3, 4, 5}
 
 
 def test_fx_non_unitary_gates_run_natively():

@@ -153,3 +153,24 @@ def test_fused_circuits_against_oracle(tensor_cores, N, fusion_k, monkeypatch):
     tensor_cores.call("qf_set_fx_tensor_cores", 0)
     alt = circ.run(qf.zero_state(N), fusion_k=fusion_k).asarray().reshape(-1)
     assert float(np.max(np.abs(alt - ref))) < TOL
+
+
+@pytest.mark.parametrize("n", [11, 14])
+def test_three_and_four_qubit_gates_against_oracle(tensor_cores, n):
+    """Unitary gates on 3 and 4 qubits (dense, and permutations with phases
+    such as CCNOT) run as tensor-core windows of their own: against the
+    oracle at 1e-12, in and out of place."""
+    rng = np.random.default_rng(60 + n)
+    st = _rand_state(n, rng)
+    gates = [np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0],
+             np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))[0],
+             orc.CCNOT(),
+             np.diag(np.exp(1j * rng.uniform(0, 2 * np.pi, 8)))[[3, 1, 2, 0, 6, 7, 4, 5]]]
+    for i, u in enumerate(gates):
+        k = int(np.log2(u.shape[0]))
+        axes = [int(a) for a in rng.choice(n, k, replace=False)]
+        for inplace in (False, True):
+            got = _apply(st, u, axes, inplace)
+            ref = orc.tensormul(np.asarray(u, dtype=np.complex128), st.reshape([2] * n), axes).reshape(-1)
+            assert np.max(np.abs(got - ref)) < TOL, (i, axes, inplace)
+

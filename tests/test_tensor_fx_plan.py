@@ -78,3 +78,23 @@ def test_sign_placement(nat):
         assert _kinds(nat, c, N, fusion_k=4) == [6], c
     k = _kinds(nat, between, N, fusion_k=4)
     assert 6 not in k and k, k
+
+
+def test_three_and_four_qubit_gates_take_the_tensor_cores(nat):
+    """A unitary gate on 3 or 4 qubits (a dense unitary, or a permutation
+    with phases such as CCNOT) is one tensor-core window of its own; below
+    2^11 amplitudes, or with the switch off, it runs in native FP64 (plan
+    kind 5)."""
+    import quantumflow_gb300 as qf
+    rng = np.random.default_rng(4)
+    u3 = np.linalg.qr(rng.normal(size=(8, 8)) + 1j * rng.normal(size=(8, 8)))[0]
+    u4 = np.linalg.qr(rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16)))[0]
+    circ = qf.Circuit([qf.H(0), qf.CCNOT(1, 5, 9), qf.Gate(u3, qubits=(2, 7, 11)),
+                       qf.Gate(u4, qubits=(3, 4, 12, 13)), qf.CNOT(0, 1)])
+    k = _kinds(nat, circ, 16)
+    assert k.count(6) >= 3 and 5 not in k, k
+    small = qf.Circuit([qf.H(0), qf.CCNOT(1, 5, 9), qf.Gate(u3, qubits=(2, 7, 8)),
+                        qf.Gate(u4, qubits=(3, 4, 6, 0))])
+    assert _kinds(nat, small, 10).count(5) == 3
+    nat.call("qf_set_fx_tensor_cores", 0)
+    assert _kinds(nat, circ, 16).count(5) == 3
