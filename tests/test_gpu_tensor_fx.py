@@ -174,3 +174,36 @@ def test_three_and_four_qubit_gates_against_oracle(tensor_cores, n):
             ref = orc.tensormul(np.asarray(u, dtype=np.complex128), st.reshape([2] * n), axes).reshape(-1)
             assert np.max(np.abs(got - ref)) < TOL, (i, axes, inplace)
 
+
+
+def test_extreme_rows_bit_exact_against_model(tensor_cores):
+    """Rows over the whole exponent range: all-zero rows, rows whose largest
+    part is below 2^-959 (they become 0, as in the CUDA-core fixed point),
+    rows near 2^900 and rows with parts 600 binades apart -- bit for bit
+    against the CPU model."""
+    n = 11
+    rng = np.random.default_rng(77)
+    st = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+    scale = np.ones(2 ** n)
+    gb = [n - 1 - a for a in (4, 9)]
+    wb = gb + [b for b in range(n - 1, -1, -1) if b not in gb][:2]
+    wmask = sum(1 << w for w in wb)
+    bases = [b for b in range(2 ** n) if not b & wmask]
+    off = [sum(((c >> j) & 1) << wb[j] for j in range(4)) for c in range(16)]
+    for i, base in enumerate(bases):
+        kind = i % 5
+        idx = [base | o for o in off]
+        if kind == 0:
+            scale[idx] = 0.0
+        elif kind == 1:
+            scale[idx] = 1e-300
+        elif kind == 2:
+            scale[idx] = 2.0 ** 900
+        elif kind == 3:
+            scale[idx] = 10.0 ** rng.uniform(-180, 0, 16)
+    st = st * scale
+    u = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))[0]
+    got = _apply(st, u, [4, 9])
+    want = _model(st, u, [4, 9])
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    assert np.all(np.isfinite(got))
