@@ -1046,20 +1046,63 @@ int fx_shape_launch(const FxShapeParams& P, cudaStream_t stream) {
   return check_cuda(cudaGetLastError());
 }
 
+// Double-double complex arithmetic for the pass unitary: products of the
+// gates' FP64 entries carried to ~106 bits with FMA-based error-free
+// transformations, the same on every host.
+struct Dd {
+  double hi = 0.0, lo = 0.0;
+};
+inline Dd dd_norm(double a, double b) {  // |a| >= |b| or a == 0
+  const double s = a + b;
+  return {s, b - (s - a)};
+}
+inline Dd dd_add(Dd a, Dd b) {
+  const double s = a.hi + b.hi, bb = s - a.hi;
+  const double e = (a.hi - (s - bb)) + (b.hi - bb) + a.lo + b.lo;
+  return dd_norm(s, e);
+}
+inline Dd dd_neg(Dd a) { return {-a.hi, -a.lo}; }
+inline Dd dd_mul_d(Dd a, double b) {
+  const double p = a.hi * b;
+  return dd_norm(p, std::fma(a.hi, b, -p) + a.lo * b);
+}
+struct Cdd {
+  Dd re, im;
+};
+inline bool cdd_zero(const Cdd& v) { return v.re.hi == 0.0 && v.im.hi == 0.0; }
+// g * v for an FP64 complex g
+inline Cdd cdd_mul(cplx g, const Cdd& v) {
+  return {dd_add(dd_mul_d(v.re, g.real()), dd_neg(dd_mul_d(v.im, g.imag()))),
+          dd_add(dd_mul_d(v.im, g.real()), dd_mul_d(v.re, g.imag()))};
+}
+inline Cdd cdd_add(const Cdd& a, const Cdd& b) { return {dd_add(a.re, b.re), dd_add(a.im, b.im)}; }
+// v * 2^62 of a double-double rounded to the nearest integer, ties away
+// from zero
+inline int64_t dd_fixed62(Dd v) {
+  const double h = std::ldexp(v.hi, 62), l = std::ldexp(v.lo, 62);
+  const double fh = std::floor(h);
+  const double frac = (h - fh) + l;  // h - fh is exact; |l| is below half an ulp of h
+  int64_t r = static_cast<int64_t>(fh);
+  if (frac > 0.5 || (frac == 0.5 && h > 0.0)) ++r;
+  else if (frac < -0.5 || (frac == -0.5 && h < 0.0)) --r;
+  return r;
+}
+
 // Fill the tensor-core pass of block B (dense unitary gates, unit-modulus
 // diagonals and phases on its window, sign ops), or return
 // QF_ERR_NOT_SUPPORTED.  The window is the block's dense bits, padded to
 // four with the highest bits outside them (the rows then keep the low
-// bits, so a warp's accesses stay contiguous).  U is multiplied up in long
-// double from the gates in block order; a sign op with bits outside the
-// window is moved to the inputs when no earlier dense gate of the block
+// bits, so a warp's accesses stay contiguous).  A sign op with bits outside
+// the window is moved to the inputs when no earlier dense gate of the block
 // touches its window bits, else to the outputs when no later one does.
-int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams& P) {
+// With `matrix` false only the structure is checked (the planner's test);
+// with it, U is multiplied up in double-double from the gates in block
+// order and rounded to the 2^-62 integers of the kernel.
+int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams& P, bool matrix = true) {
   if (B.native || B.G < 1 || B.G > 4 || n < 11) return QF_ERR_NOT_SUPPORTED;
   auto dense_op = [](const HostOp& op) {
     return op.type == OP_DENSE1 || op.type == OP_DENSE2 || op.type == OP_DENSEK || op.type == OP_MONO;
   };
-  using lcplx = std::complex<long double>;
   int wb[4], nw = 0;
   for (int j = 0; j < B.G; ++j) wb[nw++] = B.order[j];
   for (int bit = n - 1; nw < 4 && bit >= 0; --bit)
@@ -1069,8 +1112,6 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
       if (wb[j] == bit) return j;
     return -1;
   };
-  uint64_t wmask = 0;
-  for (int j = 0; j < 4; ++j) wmask |= uint64_t(1) << wb[j];
   std::memset(&P, 0, sizeof(TxParams));
   P.n = n;
   int sb[4] = {wb[0], wb[1], wb[2], wb[3]};
@@ -1082,8 +1123,13 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
       if ((c >> j) & 1) o |= int64_t(1) << wb[j];
     P.off[c] = o;
   }
-  std::vector<lcplx> U(256, lcplx(0, 0)), T(256);
-  for (int c = 0; c < 16; ++c) U[c * 16 + c] = 1;
+  std::vector<Cdd> U, T;
+  bool identity = true;  // U is still the identity (the first dense gate is copied, not multiplied)
+  if (matrix) {
+    U.assign(256, Cdd());
+    T.assign(256, Cdd());
+    for (int c = 0; c < 16; ++c) U[c * 16 + c].re.hi = 1.0;
+  }
   // window bits each dense op of the block touches, for the sign placement
   std::vector<int> dense_pos;
   std::vector<uint32_t> dense_bits;
@@ -1105,6 +1151,7 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
         jp[j] = pos(op.gb[j]);
         if (jp[j] < 0) return QF_ERR_NOT_SUPPORTED;
       }
+      if (!matrix) continue;
       const int D = 1 << op.k;
       const std::vector<cplx> gm = dense_matrix(op);
       uint32_t om = 0;
@@ -1114,26 +1161,47 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
         for (int j = 0; j < op.k; ++j) r = (r << 1) | ((c >> jp[j]) & 1);
         return r;
       };
-      // T = E U with E the gate embedded in the window
-      for (int r = 0; r < 16; ++r)
+      auto spread = [&](int r, int m) {  // window index r with the gate's bits set to m
+        int cm = r & ~static_cast<int>(om);
+        for (int j = 0; j < op.k; ++j)
+          if ((m >> (op.k - 1 - j)) & 1) cm |= 1 << jp[j];
+        return cm;
+      };
+      if (identity) {  // U = E: the gate embedded in the window
+        for (int r = 0; r < 16; ++r)
+          for (int c = 0; c < 16; ++c) {
+            Cdd v;
+            if ((r & ~static_cast<int>(om)) == (c & ~static_cast<int>(om))) {
+              const cplx g = gm[local(r) * D + local(c)];
+              v.re.hi = g.real();
+              v.im.hi = g.imag();
+            }
+            U[r * 16 + c] = v;
+          }
+        identity = false;
+        continue;
+      }
+      // T = E U
+      for (int r = 0; r < 16; ++r) {
+        const int lr = local(r);
         for (int c = 0; c < 16; ++c) {
-          lcplx acc(0, 0);
-          const int lr = local(r);
+          Cdd acc;
           for (int m = 0; m < D; ++m) {
-            int cm = r & ~static_cast<int>(om);
-            for (int j = 0; j < op.k; ++j)
-              if ((m >> (op.k - 1 - j)) & 1) cm |= 1 << jp[j];
             const cplx g = gm[lr * D + m];
-            acc += lcplx(g.real(), g.imag()) * U[cm * 16 + c];
+            const Cdd& u = U[spread(r, m) * 16 + c];
+            if ((g.real() == 0.0 && g.imag() == 0.0) || cdd_zero(u)) continue;
+            acc = cdd_add(acc, cdd_mul(g, u));
           }
           T[r * 16 + c] = acc;
         }
+      }
       U.swap(T);
       continue;
     }
     if (op.type == OP_PHASE) {
-      const lcplx s(op.scalar.real(), op.scalar.imag());
-      for (lcplx& v : U) v *= s;
+      if (!matrix) continue;
+      for (Cdd& v : U) v = cdd_mul(op.scalar, v);
+      identity = false;
       continue;
     }
     if (op.type == OP_DIAG) {
@@ -1142,12 +1210,13 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
         jp[j] = pos(op.gb[j]);
         if (jp[j] < 0) return QF_ERR_NOT_SUPPORTED;
       }
+      if (!matrix) continue;
       for (int r = 0; r < 16; ++r) {
         int e = 0;
         for (int j = 0; j < op.k; ++j) e = (e << 1) | ((r >> jp[j]) & 1);
-        const lcplx d(op.diag[e].real(), op.diag[e].imag());
-        for (int c = 0; c < 16; ++c) U[r * 16 + c] *= d;
+        for (int c = 0; c < 16; ++c) U[r * 16 + c] = cdd_mul(op.diag[e], U[r * 16 + c]);
       }
+      identity = false;
       continue;
     }
     if (op.type != OP_SIGN) return QF_ERR_NOT_SUPPORTED;
@@ -1162,9 +1231,11 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
     for (int c = 0; c < 16; ++c)
       if ((c & jm) == jm) rm |= 1u << c;
     if (mo == 0) {  // inside the window: a diagonal of U
+      if (!matrix) continue;
       for (int r = 0; r < 16; ++r)
         if ((rm >> r) & 1)
-          for (int c = 0; c < 16; ++c) U[r * 16 + c] = -U[r * 16 + c];
+          for (int c = 0; c < 16; ++c) U[r * 16 + c] = {dd_neg(U[r * 16 + c].re), dd_neg(U[r * 16 + c].im)};
+      identity = false;
       continue;
     }
     bool before = false, after = false;
@@ -1185,13 +1256,15 @@ int tx_prepare(int n, const std::vector<HostOp>& ops, const FxBlock& B, TxParams
       return QF_ERR_NOT_SUPPORTED;
     }
   }
-  (void)wmask;
+  if (!matrix) return QF_OK;
   for (int r = 0; r < 16; ++r)
     for (int c = 0; c < 16; ++c) {
-      const lcplx v = U[r * 16 + c];
-      if (std::abs(v.real()) > 1.0L + 1e-9L || std::abs(v.imag()) > 1.0L + 1e-9L) return QF_ERR_NOT_SUPPORTED;
-      P.g[r][c][0] = std::llround(std::ldexp(v.real(), 62));
-      P.g[r][c][1] = std::llround(std::ldexp(v.imag(), 62));
+      const Cdd& v = U[r * 16 + c];
+      // unit rows of a product of gates unitary to 1e-9: well inside the
+      // digits' bounds (|G| < 2^62.9 keeps G + bias below 2^64)
+      if (std::abs(v.re.hi) > 1.0 + 1e-6 || std::abs(v.im.hi) > 1.0 + 1e-6) return QF_ERR_NOT_SUPPORTED;
+      P.g[r][c][0] = dd_fixed62(v.re);
+      P.g[r][c][1] = dd_fixed62(v.im);
     }
   return QF_OK;
 }
@@ -1208,14 +1281,14 @@ std::vector<FxBlock> fx_plan_final(std::vector<HostOp>& ops, int n, int& fusion_
   static thread_local TxParams tp;  // ~5 KiB: kept off the stack
   for (FxBlock& B : blocks) {
     if (B.wide) {  // a 3- or 4-qubit gate: alone on the tensor cores, else native FP64
-      if (tx_prepare(n, ops, B, tp) == QF_OK) B.shape = -2;
+      if (tx_prepare(n, ops, B, tp, false) == QF_OK) B.shape = -2;
       else B.native = true;
       out.push_back(std::move(B));
       continue;
     }
     // a lone 2x2 gate streams faster through the CUDA-core sweep
     const bool lone2x2 = B.idx.size() == 1 && ops[B.idx[0]].type == OP_DENSE1;
-    if (!lone2x2 && tx_prepare(n, ops, B, tp) == QF_OK) {
+    if (!lone2x2 && tx_prepare(n, ops, B, tp, false) == QF_OK) {
       B.shape = -2;
       out.push_back(std::move(B));
       continue;

@@ -53,6 +53,30 @@ def test_tensormul_against_oracle(N, K):
     assert np.max(np.abs(bk.evaluate(out) - ref)) < 1e-12 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("K", [2, 3, 4])
+def test_unitary_tensormul_on_tensor_cores(K):
+    """Unitary gates through the backend module on a 12-qubit state: the
+    complex128 tensor-core pass (unmodified reference code reaches it
+    through Gate.run -> bk.tensormul)."""
+    import quantumflow_gb300.refbackend as bk
+    from quantumflow_gb300 import _native as nat
+    rng = np.random.default_rng(90 + K)
+    N = 12
+    state = rng.normal(size=[2] * N) + 1j * rng.normal(size=[2] * N)
+    gate = np.linalg.qr(rng.normal(size=(2 ** K, 2 ** K)) + 1j * rng.normal(size=(2 ** K, 2 ** K)))[0]
+    idx = [int(i) for i in rng.choice(N, size=K, replace=False)]
+    nat.timing_collect()
+    nat.timing_enable(True)
+    try:
+        out = bk.tensormul(bk.astensorproduct(gate.reshape([2] * (2 * K))), bk.astensorproduct(state), idx)
+        res = bk.evaluate(out)
+    finally:
+        nat.timing_enable(False)
+    assert nat.timing_collect()["fx_tensor"][1] == 1
+    ref = orc.tensormul(gate, state, idx)
+    assert np.max(np.abs(res - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
 def test_reference_fixture_tensormul(golden):
     import quantumflow_gb300.refbackend as bk
     g = golden["tensormul"]
