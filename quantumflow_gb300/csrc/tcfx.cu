@@ -5,9 +5,10 @@
 // Reference semantics: quantumflow/backend/numpybk.py:159-214 tensormul
 // applied gate by gate (quantumflow/circuits.py:87-99).  A pass applies a
 // run of unitary gates whose dense qubits lie in a window of four bits,
-// with CZ-like sign ops around them: the host multiplies them into one
-// 16x16 unitary U (long double) and the pass computes y = U x for every
-// "row" x, the 16 amplitudes that differ only in the window bits.
+// with CZ-like sign ops around them (or one unitary gate on 3 or 4
+// qubits): the host multiplies them into one 16x16 unitary U (double-double)
+// and the pass computes y = U x for every "row" x, the 16 amplitudes that
+// differ only in the window bits.
 //
 // Arithmetic (an integer form of the Ozaki splitting scheme: Ozaki, Ogita,
 // Oishi and Rump, "Error-free transformations of matrix multiplication by
@@ -19,9 +20,10 @@
 //    FP64 pipe is the narrowest unit on this part);
 //  * U's real form (32 x 32) is G = round(g * 2^62), |G| <= 2^62;
 //  * both are written in base 256 with balanced digits: X + 0x8080..80 =
-//    sum_t (d_t + 128) 256^(7-t), d_t in [-128, 127], so a byte of the
-//    biased integer is a digit (one byte permute per digit pair) and every
-//    digit is exact in fp16;
+//    sum_t (d_t + 128) 256^(7-t), d_t in [-128, 127] (the amplitudes'
+//    top byte is biased by 0x40 instead, which keeps it below 0x80), so a
+//    byte of the biased integer is a digit (one byte permute per digit
+//    pair) and every digit is exact in fp16;
 //  * A.G = sum_delta acc_delta 256^(14 - delta), acc_delta = sum over the
 //    digit pairs t + u = delta of the digit GEMMs; delta = 0..7 are kept
 //    (36 of the 64 digit products).  With K = 32 terms per output every
@@ -47,10 +49,11 @@
 // turn their amplitudes into digits and store them as the A operand, K-major
 // rows of 8 digits x 32 reals in four 128-byte swizzled chunks.  The gate's
 // digits (B: 8 digit blocks x 32 output reals, K = 32 input reals) are built
-// once per CTA.  Thread 0 issues, per amplitude digit t, two MMAs (K = 16
-// each) against the first 32 (8 - t) rows of B into tensor-memory columns
-// [32 t, 256) of the stage: column block delta receives every digit product
-// of its weight.  Warps 8-15 run the epilogue: the thread of TMEM lane r
+// once per CTA.  Once every converter has arrived on the stage's mbarrier,
+// thread 0 issues, per amplitude digit t, two MMAs (K = 16 each) against
+// the first 32 (8 - t) rows of B into tensor-memory columns [32 t, 256) of
+// the stage: column block delta receives every digit product of its
+// weight.  Warps 8-15 run the epilogue: the thread of TMEM lane r
 // (two per row, 16 output reals each) reads the eight accumulators of each
 // output, combines them into Z and stores FP64.  Conversion, MMAs and
 // epilogue of consecutive tiles overlap.  Every wait is bounded (4 s): on
