@@ -43,22 +43,23 @@
 // FP64 arithmetic on the same row.  The CPU model of this arithmetic
 // (tests/txarith.py) measures it against exact rational arithmetic.
 //
-// Kernel: one CTA of 512 threads per SM, persistent over tiles of 128 rows
-// (the MMA's M), two stages.  Warps 0-7 convert: two threads per row (lanes
-// l and l ^ 8, eight amplitudes each; the row exponent is a shuffle away)
-// turn their amplitudes into digits and store them as the A operand, K-major
-// rows of 8 digits x 32 reals in four 128-byte swizzled chunks.  The gate's
-// digits (B: 8 digit blocks x 32 output reals, K = 32 input reals) are built
-// once per CTA.  Once every converter has arrived on the stage's mbarrier,
-// thread 0 issues, per amplitude digit t, two MMAs (K = 16 each) against
-// the first 32 (8 - t) rows of B into tensor-memory columns [32 t, 256) of
-// the stage: column block delta receives every digit product of its
-// weight.  Warps 8-15 run the epilogue: the thread of TMEM lane r
-// (two per row, 16 output reals each) reads the eight accumulators of each
-// output, combines them into Z and stores FP64.  Conversion, MMAs and
-// epilogue of consecutive tiles overlap.  Every wait is bounded (4 s): on
-// expiry the kernel raises the device error word and every thread leaves
-// its loop.
+// Kernel: one CTA of 640 threads per SM, persistent over tiles of 128 rows
+// (the MMA's M); three stages of the A operand, two of the accumulators.
+// Warps 0-7 convert: two threads per row (lanes l and l ^ 8, eight
+// amplitudes each; the row exponent is a shuffle away) turn their
+// amplitudes into digits and store them as the A operand, K-major rows of
+// 8 digits x 32 reals in four 128-byte swizzled chunks.  The gate's digits
+// (B: 8 digit blocks x 32 output reals, K = 32 input reals) are built once
+// per CTA.  Once every converter has arrived on the stage's mbarrier, the
+// first thread of warps 16-19 issues, per amplitude digit t, two MMAs
+// (K = 16 each) against the first 32 (8 - t) rows of B into tensor-memory
+// columns [32 t, 256) of the accumulator stage: column block delta
+// receives every digit product of its weight.  Warps 8-15 run the
+// epilogue: the thread of TMEM lane r (two per row, 16 output reals each)
+// reads the eight accumulators of each output, combines them into Z and
+// stores FP64.  Conversion, MMAs and epilogue of consecutive tiles overlap.
+// Every wait is bounded (4 s): on expiry the kernel raises the device error
+// word and every thread leaves its loop.
 #include <algorithm>
 #include <atomic>
 #include <cstring>
@@ -335,7 +336,7 @@ QF_D int tx_rowexp(const double2 (&x)[AP]) {
 // are in flight during the rest of this conversion and the MMAs.
 template <int AP>
 QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 (&x)[AP], unsigned char* sa,
-                     int* rowE, int64_t b, int irow, int q, int E, int64_t nb) {
+                     uint16_t* rowE, int64_t b, int irow, int q, int E, int64_t nb) {
   if (P.nin > 0) {
     uint32_t fl = 0u;
     for (int s = 0; s < P.nin; ++s)
@@ -348,7 +349,7 @@ QF_D void tx_convert(const TxParams& P, const double2* __restrict__ in, double2 
                           fx_double(fx_hiword(x[j].y) ^ sg, fx_loword(x[j].y)));
     }
   }
-  if (q == 0) rowE[irow] = E;
+  if (q == 0) rowE[irow] = static_cast<uint16_t>(E);
   const uint32_t Ep = static_cast<uint32_t>(E + 64 - TX_MB);
 #pragma unroll
   for (int j0 = 0; j0 < AP; j0 += 4) {
@@ -455,43 +456,63 @@ QF_D void tx_arrive(uint64_t* bar) {
 }
 
 // ------------------------------------------------ warp-specialised kernel ----
-// One CTA per SM, two stages of A, rowE and accumulators.  The converter
-// warps (AP amplitudes per thread: 8 -> 8 warps, 4 -> 16 warps) convert
-// tile i into stage i & 1 (after the epilogue of tile i - 2 released it)
-// and arrive on a_full[stage]; thread 0 waits for all of them and issues
-// the tile's MMAs, committed to mma_done[stage], while the other converter
-// warps go on with their next tile.  The 8 epilogue warps wait for both
-// barriers, run the epilogue from the stage's accumulators and release the
-// stage (tmem_free, one arrival per warp).
-constexpr uint32_t TP_SMEM = 2 * TX_A_BYTES + TX_B_BYTES + 1024;
+// One CTA per SM; three stages of the A operand (tile i in A stage i % 3),
+// two of the accumulators (tensor-memory stage i & 1: 2 x 256 of its 512
+// columns).  The converter warps (AP amplitudes per thread: 8 -> 8 warps,
+// 4 -> 16 warps) convert tile i into its A stage once the MMAs of tile i - 3
+// have read it (a_free) and arrive on a_full.  One thread of the last warp
+// issues the MMAs: it waits for the converters of tile i and for the
+// epilogue of tile i - 2 to release the accumulators (tmem_free), issues
+// the tile's MMAs and commits them to a_free and mma_done.  An MMA issue
+// holds its thread about as long as the tensor core takes to run it, so
+// that thread does nothing else.  The 8 epilogue warps wait for the MMAs
+// (and for the issuer's e_ready, which passes on the converters' row
+// exponents), run the epilogue from the accumulators and release them
+// (tmem_free, one arrival per warp).  The converters wait only for the
+// tensor core, the epilogue only for the MMAs.
+constexpr int TX_AST = 3;   // A-operand stages
+constexpr int TX_ESL = 5;   // row-exponent slots: tile i + 5 is converted only after the epilogue of tile i
+constexpr uint32_t TP_SMEM = TX_AST * TX_A_BYTES + TX_B_BYTES + 1024;
 constexpr int TP_TMEM_COLS = 512;
 
 template <int AP>
 struct TxShape {
   static constexpr int CW = 128 * (16 / AP) / 32;  // converter warps
-  static constexpr int THREADS = 32 * (CW + 8);
+  // converters, epilogue, and one warpgroup whose first thread issues the MMAs
+  static constexpr int THREADS = 32 * (CW + 8 + 4);
   static constexpr bool DB = AP == 8;               // double-buffered tensor-memory reads (registers allow)
 };
+// Register split (AP = 8: 640 threads launched at 96 registers, 61440 in
+// all): the issuer's warpgroup gives its registers up (24 each) and the
+// converters take 128; 256 x 128 + 256 x 96 (epilogue) + 128 x 24 = 60416.
+constexpr int TX_REG_LAUNCH = 96, TX_REG_CONV = 128, TX_REG_ISSUE = 24;
+static_assert(256 * TX_REG_CONV + 256 * TX_REG_LAUNCH + 128 * TX_REG_ISSUE <= 640 * TX_REG_LAUNCH,
+              "register split above the launch's registers");
+static_assert(32 * (2 * TX_REG_CONV + 2 * TX_REG_LAUNCH + TX_REG_ISSUE) <= 16384,
+              "register split above one scheduler partition's registers");
 
 template <int AP>
 __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid_constant__ TxParams P) {
   constexpr int CW = TxShape<AP>::CW;
   extern __shared__ __align__(1024) unsigned char tx_raw[];
-  unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tx_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* sb = sm + 2 * TX_A_BYTES;
-  __shared__ __align__(8) uint64_t mma_done[2], a_full[2], tmem_free[2];
+  unsigned char* sm = tx_raw + ((1024u - (tx_smem(tx_raw) & 1023u)) & 1023u);  // 1024-byte aligned
+  unsigned char* sb = sm + TX_AST * TX_A_BYTES;
+  __shared__ __align__(8) uint64_t a_full[TX_AST], a_free[TX_AST], mma_done[2], e_ready[2], tmem_free[2];
   __shared__ uint32_t tmem_slot;
-  __shared__ int rowE[2][TX_ROWS];
+  __shared__ uint16_t rowE[TX_ESL][TX_ROWS];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   tx_build_b(P, sb, tid, TxShape<AP>::THREADS);
   if (warp == 0) tx_alloc(&tmem_slot, TP_TMEM_COLS);
   if (tid == 0) {
-    tx_bar_init(&mma_done[0], 1);
-    tx_bar_init(&mma_done[1], 1);
-    tx_bar_init(&a_full[0], 32 * CW);
-    tx_bar_init(&a_full[1], 32 * CW);
-    tx_bar_init(&tmem_free[0], 8);
-    tx_bar_init(&tmem_free[1], 8);
+    for (int a = 0; a < TX_AST; ++a) {
+      tx_bar_init(&a_full[a], 32 * CW);
+      tx_bar_init(&a_free[a], 1);
+    }
+    for (int t = 0; t < 2; ++t) {
+      tx_bar_init(&mma_done[t], 1);
+      tx_bar_init(&e_ready[t], 1);
+      tx_bar_init(&tmem_free[t], 8);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -501,12 +522,12 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
   const uint32_t tmem = tmem_slot;
   const int64_t ntiles = (int64_t(1) << (P.n - 4)) / TX_ROWS;
   if (warp < CW) {
-    // ---- converters and the MMA issuer.  Row irow, group q (window
+    if constexpr (AP == 8) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(TX_REG_CONV));
+    // ---- converters.  Row irow, group q (window
     // indices AP q .. AP q + AP - 1); the lanes of one 8-lane shared-store
     // phase hold 8 consecutive rows (distinct swizzle phases) and the groups
     // of a row are lanes l ^ 8 (and l ^ 16, l ^ 24)
     const double2* __restrict__ in = static_cast<const double2*>(P.in);
-    const uint32_t bbase = tx_smem(sb);
     const int irow = AP == 8 ? warp * 16 + (lane & 7) + ((lane >> 4) << 3) : warp * 8 + (lane & 7);
     const int q = AP == 8 ? (lane >> 3) & 1 : lane >> 3;
     const int64_t grow = tx_spread(P, irow) | P.off[AP * q];  // this group within its tile
@@ -518,31 +539,44 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
 #pragma unroll
       for (int j = 0; j < AP; ++j) x[j] = in[b | P.off[j]];
     }
-    int fail = 0;
+    int a = 0, ar = 0;  // A stage (it % 3) and its round (it / 3)
     for (int it = 0; tile < ntiles; tile += step, ++it) {
-      const int s = it & 1;
       bool ok = true;
-      if (it >= 2) ok = tx_wait(&tmem_free[s], static_cast<uint32_t>((it >> 1) - 1) & 1u, P.err);
-      if (!__all_sync(0xffffffffu, ok)) fail = 1;  // warp-uniform: the row exponent shuffles within the warp
+      if (ar > 0) ok = tx_wait(&a_free[a], static_cast<uint32_t>(ar - 1) & 1u, P.err);
+      if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform: the row exponent shuffles within the warp
       tx_fence_after();
-      unsigned char* sa = sm + s * TX_A_BYTES;
+      unsigned char* sa = sm + a * TX_A_BYTES;
       const int64_t nb = tile + step < ntiles ? tx_spread(P, (tile + step) * TX_ROWS) | grow : -1;
-      if (!fail)
-        tx_convert<AP>(P, in, x, sa, rowE[s], tx_spread(P, tile * TX_ROWS) | grow, irow, q, tx_rowexp<AP>(x), nb);
-      if (fail) break;
+      tx_convert<AP>(P, in, x, sa, rowE[it % TX_ESL], tx_spread(P, tile * TX_ROWS) | grow, irow, q,
+                     tx_rowexp<AP>(x), nb);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tx_arrive(&a_full[s]);  // this thread's digits and row exponent are written
-      if (warp == 0) {
-        // warp 0 issues the tile's MMAs once every converter has arrived; the
-        // other converter warps go straight on to their next tile
-        bool issued = false;
-        if (lane == 0 && tx_wait(&a_full[s], static_cast<uint32_t>(it >> 1) & 1u, P.err)) {
-          tx_fence_after();
-          tx_issue(tx_smem(sa), bbase, tmem + static_cast<uint32_t>(256 * s));
-          tx_commit(&mma_done[s]);
-          issued = true;
+      tx_arrive(&a_full[a]);  // this thread's digits and row exponent are written
+      if (++a == TX_AST) {
+        a = 0;
+        ++ar;
+      }
+    }
+  } else if (warp >= CW + 8) {
+    // ---- MMA issuer (one thread of this warpgroup)
+    if constexpr (AP == 8) asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(TX_REG_ISSUE));
+    if (warp == CW + 8 && lane == 0) {
+      const uint32_t bbase = tx_smem(sb);
+      int a = 0, ar = 0;
+      for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int t = static_cast<int>(it & 1);
+        if (!tx_wait(&a_full[a], static_cast<uint32_t>(ar) & 1u, P.err)) break;
+        if (it >= 2 && !tx_wait(&tmem_free[t], static_cast<uint32_t>((it >> 1) - 1) & 1u, P.err)) break;
+        // the converters' row exponents, passed on to the epilogue (after
+        // tmem_free, so that e_ready is never two phases ahead of it)
+        tx_arrive(&e_ready[t]);
+        tx_fence_after();
+        tx_issue(tx_smem(sm + a * TX_A_BYTES), bbase, tmem + static_cast<uint32_t>(256 * t));
+        tx_commit(&a_free[a]);
+        tx_commit(&mma_done[t]);
+        if (++a == TX_AST) {
+          a = 0;
+          ++ar;
         }
-        if (!__shfl_sync(0xffffffffu, issued ? 1 : 0, 0)) break;
       }
     }
   } else {
@@ -554,16 +588,16 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
     const uint32_t lane_addr = static_cast<uint32_t>(32 * (ew & 3)) << 16;
     int64_t tile = blockIdx.x;
     for (int it = 0; tile < ntiles; tile += gridDim.x, ++it) {
-      const int s = it & 1;
+      const int t = it & 1;
       const uint32_t par = static_cast<uint32_t>(it >> 1) & 1u;
-      const bool ok = tx_wait(&a_full[s], par, P.err) && tx_wait(&mma_done[s], par, P.err);
+      const bool ok = tx_wait(&e_ready[t], par, P.err) && tx_wait(&mma_done[t], par, P.err);
       if (!__all_sync(0xffffffffu, ok)) break;
       tx_fence_after();
-      tx_epilogue<TxShape<AP>::DB>(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * s), rowE[s][orow],
-                                   tx_spread(P, tile * TX_ROWS) | hrow, oh);
+      tx_epilogue<TxShape<AP>::DB>(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * t),
+                                   rowE[it % TX_ESL][orow], tx_spread(P, tile * TX_ROWS) | hrow, oh);
       tx_fence_before();
       __syncwarp();
-      if (lane == 0) tx_arrive(&tmem_free[s]);
+      if (lane == 0) tx_arrive(&tmem_free[t]);
     }
   }
   tx_fence_before();
