@@ -122,6 +122,17 @@ QF_D void tx_commit(uint64_t* bar) {
 }
 QF_D void tx_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 QF_D void tx_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+QF_D void tx_alloc(uint32_t* slot, uint32_t cols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tx_smem(slot)), "r"(cols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+QF_D void tx_bar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tx_smem(bar)), "r"(count) : "memory");
+}
+QF_D void tx_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tx_smem(bar)) : "memory");
+}
 
 // waits for the phase to complete, suspended up to about 100 us per try
 QF_D bool tx_try_wait(uint64_t* bar, uint32_t parity) {
@@ -405,9 +416,11 @@ QF_D void tx_issue(uint32_t abase, uint32_t bbase, uint32_t acc) {
 // Epilogue of one thread: 16 output reals (amplitudes c = 8 oh + j) of its
 // row (half-row base b) from the accumulators at tensor-memory address acc
 // (lane field set), with the output-side signs, stored as FP64.  The tensor-memory loads of
-// the next four reals are in flight while four are converted.
+// the next four reals are in flight while four are converted.  As soon as
+// the last of them has landed, the warp releases the accumulators (one
+// arrival on tmem_free), before its last conversions and stores.
 template <bool DB>
-QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int64_t b, int oh) {
+QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int64_t b, int oh, uint64_t* tmem_free) {
   const uint32_t delta = static_cast<uint32_t>(E - 1082) << 20;
   uint32_t fl = 0u;
   for (int s = 0; s < P.nout; ++s)
@@ -423,6 +436,11 @@ QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int6
       for (int d = 0; d < 8; ++d) tx_ld4(acc + static_cast<uint32_t>(TX_KD * d + 16 * oh + 4 * q), a4[0][d]);
     }
     tx_wait_ld(a4[DB ? (q & 1) : 0]);
+    if (q == 3) {
+      tx_fence_before();
+      __syncwarp();
+      if ((threadIdx.x & 31) == 0) tx_arrive(tmem_free);
+    }
     if (DB && q < 3) {
 #pragma unroll
       for (int d = 0; d < 8; ++d)
@@ -441,18 +459,6 @@ QF_D void tx_epilogue(const TxParams& P, double2* out, uint32_t acc, int E, int6
       out[b | P.off[j]] = make_double2(tx_out(tx_combine(wr), ds), tx_out(tx_combine(wi), ds));
     }
   }
-}
-
-QF_D void tx_alloc(uint32_t* slot, uint32_t cols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tx_smem(slot)), "r"(cols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-QF_D void tx_bar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tx_smem(bar)), "r"(count) : "memory");
-}
-QF_D void tx_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tx_smem(bar)) : "memory");
 }
 
 // ------------------------------------------------ warp-specialised kernel ----
@@ -483,12 +489,13 @@ struct TxShape {
   static constexpr bool DB = AP == 8;               // double-buffered tensor-memory reads (registers allow)
 };
 // Register split (AP = 8: 640 threads launched at 96 registers, 61440 in
-// all): the issuer's warpgroup gives its registers up (24 each) and the
-// converters take 128; 256 x 128 + 256 x 96 (epilogue) + 128 x 24 = 60416.
-constexpr int TX_REG_LAUNCH = 96, TX_REG_CONV = 128, TX_REG_ISSUE = 24;
-static_assert(256 * TX_REG_CONV + 256 * TX_REG_LAUNCH + 128 * TX_REG_ISSUE <= 640 * TX_REG_LAUNCH,
+// all): the issuer's warpgroup gives its registers up (24 each), the
+// converters take 120 and the epilogue 104: 256 x 120 + 256 x 104 + 128 x 24
+// = 60416 (at N=28, 128 / 96 ran 1.5% and 112 / 112 0.7% slower).
+constexpr int TX_REG_LAUNCH = 96, TX_REG_CONV = 120, TX_REG_EPI = 104, TX_REG_ISSUE = 24;
+static_assert(256 * TX_REG_CONV + 256 * TX_REG_EPI + 128 * TX_REG_ISSUE <= 640 * TX_REG_LAUNCH,
               "register split above the launch's registers");
-static_assert(32 * (2 * TX_REG_CONV + 2 * TX_REG_LAUNCH + TX_REG_ISSUE) <= 16384,
+static_assert(32 * (2 * TX_REG_CONV + 2 * TX_REG_EPI + TX_REG_ISSUE) <= 16384,
               "register split above one scheduler partition's registers");
 
 template <int AP>
@@ -581,6 +588,7 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
     }
   } else {
     // ---- epilogue
+    if constexpr (AP == 8) asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(TX_REG_EPI));
     double2* out = static_cast<double2*>(P.out);
     const int ew = warp - CW;
     const int orow = 32 * (ew & 3) + lane, oh = ew >> 2;
@@ -594,10 +602,7 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
       if (!__all_sync(0xffffffffu, ok)) break;
       tx_fence_after();
       tx_epilogue<TxShape<AP>::DB>(P, out, tmem + lane_addr + static_cast<uint32_t>(256 * t),
-                                   rowE[it % TX_ESL][orow], tx_spread(P, tile * TX_ROWS) | hrow, oh);
-      tx_fence_before();
-      __syncwarp();
-      if (lane == 0) tx_arrive(&tmem_free[t]);
+                                   rowE[it % TX_ESL][orow], tx_spread(P, tile * TX_ROWS) | hrow, oh, &tmem_free[t]);
     }
   }
   tx_fence_before();
