@@ -188,21 +188,17 @@ QF_D void tx_wait_ld(uint32_t (&a)[8][4]) {
 // Biased fixed-point integer of one part: A + TX_BIAS_A, A = v * 2^(1022 +
 // 61 - E) truncated toward zero (Ep = E + 3 >= the part's exponent field +
 // 3).  The 64-bit mantissa with its hidden bit at bit 63 is shifted right by
-// n = Ep - e with clamped funnel shifts (no selects); zeros and subnormals
-// (n >= 67) shift out completely.  The sign and the bias are one add:
-// (t ^ neg) - neg + BIAS = (t ^ neg) + BIAS + (neg & 1).
+// n = Ep - e in one 64-bit shift, whose amount clamps at 64 (zeros and
+// subnormals, n >= 67, shift out completely).  The sign and the bias are
+// one add: (t ^ neg) - neg + BIAS = (t ^ neg) + BIAS + (neg & 1).
 QF_D uint64_t tx_biased(double v, uint32_t Ep) {
   const uint32_t hi = fx_hiword(v), lo = fx_loword(v);
   const uint32_t e = (hi >> 20) & 0x7ffu;
-  const uint32_t mh = __funnelshift_l(lo, hi, 11) | 0x80000000u;
-  const uint32_t ml = lo << 11;
-  const uint32_t n = Ep - e;
-  uint32_t tl = __funnelshift_rc(ml, mh, n);             // low word of m >> min(n, 32)
-  const uint32_t th = __funnelshift_rc(mh, 0u, n);        // high word (0 once n >= 32)
-  tl = __funnelshift_rc(tl, 0u, n > 32u ? n - 32u : 0u);  // the rest of a shift past 32 (0 past 64)
-  const uint32_t neg = static_cast<uint32_t>(static_cast<int32_t>(hi) >> 31);
-  const uint64_t t = (static_cast<uint64_t>(th ^ neg) << 32) | (tl ^ neg);
-  return t + TX_BIAS_A + (neg & 1u);
+  const uint64_t m = (static_cast<uint64_t>(__funnelshift_l(lo, hi, 11) | 0x80000000u) << 32) | (lo << 11);
+  uint64_t t;
+  asm("shr.b64 %0, %1, %2;" : "=l"(t) : "l"(m), "r"(Ep - e));
+  const uint64_t neg = static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(hi) >> 31));
+  return (t ^ neg) + TX_BIAS_A + (neg & 1u);
 }
 
 // fp16x2 word of digit t (0 = most significant) of two biased integers:
