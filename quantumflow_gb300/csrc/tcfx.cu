@@ -565,6 +565,7 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
     if (warp == CW + 8 && lane == 0) {
       const uint32_t bbase = tx_smem(sb);
       int a = 0, ar = 0;
+      int64_t last = -1;  // the last tile whose MMAs were issued
       for (int64_t it = 0, tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int t = static_cast<int>(it & 1);
         if (!tx_wait(&a_full[a], static_cast<uint32_t>(ar) & 1u, P.err)) break;
@@ -576,11 +577,16 @@ __global__ void __launch_bounds__(TxShape<AP>::THREADS, 1) k_txpipe(const __grid
         tx_issue(tx_smem(sm + a * TX_A_BYTES), bbase, tmem + static_cast<uint32_t>(256 * t));
         tx_commit(&a_free[a]);
         tx_commit(&mma_done[t]);
+        last = it;
         if (++a == TX_AST) {
           a = 0;
           ++ar;
         }
       }
+      // every MMA issued has finished before the accumulators are freed (on
+      // the normal path the epilogue has already seen this phase; after an
+      // expired wait the epilogue may have left its loop early)
+      if (last >= 0) tx_wait(&mma_done[last & 1], static_cast<uint32_t>(last >> 1) & 1u, P.err);
     }
   } else {
     // ---- epilogue
