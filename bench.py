@@ -82,7 +82,7 @@ KERNEL_TRAFFIC_N24 = {
     # fixed-point straight-line pass k_fxshape<4, 132, 110> (mean of 3 launches)
     "fx_shape": (268.601941e6, 208.636416e6),
     # tensor-core complex128 pass k_txpipe (one launch, --set full)
-    "fx_tensor": (268.503296e6, 212.204288e6),
+    "fx_tensor": (268.577024e6, 212.714240e6),
     "fx_group": (268.538240e6, 209.662080e6),
 }
 
